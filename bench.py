@@ -1,0 +1,424 @@
+#!/usr/bin/env python
+"""Benchmark of the tracer's hot path on one GB300 (or N replicas).
+
+Default workload: the mixed-precision forward at 1024^3 fields / nside 1024
+(12,582,912 rays) / 512 RK4 steps, synthetic Gaussian fields (P(k) ~ k^-3,
+phi rms 1e-5, transverse B rms 1e-7, seeded) generated on the GPU. A step is
+one full-sky forward trace (srt_forward) with the fields already resident in
+HBM; the headline metric is ray-steps/s = rays x n_steps / time.
+
+Also reported on the same line:
+  e2e          the same metric through the C ABI with HOST buffers: upload and
+               lay out phi and B from pinned host memory, trace, read the six
+               maps back, every step;
+  roofline     the trace kernel's FP32 issue rate (algorithmic FLOP per
+               ray-step x ray-steps / CUDA-event time of the kernel) against the
+               FP32 FMA rate measured on this GPU by srt_probe_peak;
+  compare      the plain FP64 GPU form and the reference-arithmetic (REF16) GPU
+               form on one batch of the same workload, the mixed/FP64 speed
+               ratio, and per-map errors of the mixed form against FP64;
+  cpu_baseline the FP64 CPU oracle timed on a bounded sample of rays of the
+               same workload on all host cores.
+--impl reference times the reference's own CPU arithmetic for the path on the
+host cores (oracle/_ref where it was built from the reference sources, else
+the oracle's REF16 port) on bounded samples of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "snapshot-raytracer_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+# Algorithmic work of one RK4 step of one ray (4 right-hand-side evaluations,
+# each 4 tricubic interpolations with value, gradient and Hessian):
+#   tricubic, separable: x pass 16 rows x 3 outputs x 4 taps, y pass 4 x 6 x 4,
+#     z pass 10 x 4 multiply-adds = 328 FMA = 656 FLOP, plus 3 axes x 12
+#     Catmull-Rom weights (48 FLOP per axis) = 144 FLOP  -> 800 FLOP
+#   right-hand side outside the interpolations (unit vectors, projections, B
+#     tidal terms, Sachs equations)                         -> 330 FLOP
+#   RK4 stage states and accumulation, 19 components        -> 152 FLOP
+FLOP_PER_RAY_STEP = 4 * (4 * 800 + 330) + 152          # = 14,272
+# Bytes gathered per ray-step: 4 stages x 4 fields x 64 taps x 4 B (FP32 fields).
+GATHER_BYTES_PER_RAY_STEP = 4 * 4 * 64 * 4               # = 4,096
+MAP_NAMES = ("dA", "ellipticity1", "ellipticity2", "rotation", "deflection1", "deflection2")
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=1024, help="grid side")
+    ap.add_argument("--nside", type=int, default=1024)
+    ap.add_argument("--n-steps", type=int, default=512)
+    ap.add_argument("--precision", default="mixed", choices=("mixed", "fp64", "ref16"))
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--compare-batch", type=int, default=5, help="batch used for the FP64 / REF16 legs (-1: skip)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
+    ap.add_argument("--oracle-sample", type=int, default=24, help="pixels checked against the FP64 oracle")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(name)
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+
+def dist_setup(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def map_errors(a, b):
+    out = {}
+    for m, name in enumerate(MAP_NAMES):
+        d = a[m].astype(np.float64) - b[m].astype(np.float64)
+        r = b[m].astype(np.float64)
+        if m == 0:
+            r = r - r.mean()
+        s = max(float(np.sqrt(np.mean(r * r))), 1e-300)
+        out[name] = {"rms_rel": float(np.sqrt(np.mean(d * d)) / s), "max_rel": float(np.abs(d).max() / s)}
+    return out
+
+
+def sample_pixels(nside, count, begin=0, total=None, seed=0):
+    total = 12 * nside * nside - begin if total is None else total
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(total, size=min(count, total), replace=False)) + begin
+
+
+def time_cpu(fn, target_s, make_sample, start=16):
+    """Grow the sample until one call takes >= target_s / 4, then scale to
+    ~target_s; returns (rays, seconds)."""
+    n = start
+    while True:
+        pix = make_sample(n)
+        t0 = time.perf_counter()
+        fn(pix)
+        dt = time.perf_counter() - t0
+        if dt >= target_s / 4 or n >= 1 << 20:
+            break
+        n = int(n * max(2.0, min(16.0, (target_s / 4) / max(dt, 1e-3))))
+    if dt < target_s * 0.75:
+        n = int(n * target_s / max(dt, 1e-3))
+        pix = make_sample(n)
+        t0 = time.perf_counter()
+        fn(pix)
+        dt = time.perf_counter() - t0
+    return len(pix), dt
+
+
+# --------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import torch
+
+    import srt
+    import srt_fields
+
+    rank, world, local = dist_setup(args.gpus)
+    dev = torch.device("cuda", local)
+    n, nside, S = args.n, args.nside, args.n_steps
+    npix = 12 * nside * nside
+    cfg = {"workload": "forward trace, %d^3 fields, nside %d (%d rays), %d steps, %s" % (n, nside, npix, S,
+                                                                                       args.precision),
+           "grid": n, "nside": nside, "rays": npix, "n_steps": S, "precision": args.precision,
+           "fields": "gaussian P(k)~k^-3, phi rms 1e-5, B rms 1e-7, seed %d" % (args.seed + rank),
+           "l2": "inputs larger than L2 (%.1f GB of fields vs 0.13 GB L2)" % (16 * n ** 3 / 1e9),
+           "parallelism": "replicas x%d (pixel-parallel, no collective)" % world}
+
+    phi_d, b_d = srt_fields.gaussian_fields_torch(n, seed=args.seed + rank, device=dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    fields = srt.Fields(phi_d, b_d, stream=stream)
+    out = torch.empty((6, npix), dtype=torch.float32, device=dev)
+
+    peak_fp32 = srt.probe_peak("fp32")
+    peak_fp64 = srt.probe_peak("fp64")
+
+    for _ in range(args.warmup):
+        fields.forward(nside, S, precision=args.precision, out=out, stream=stream)
+    torch.cuda.synchronize()
+
+    trace_ms, kernels = [], 0
+    with ClockSampler(local) as clocks:
+        barrier(world)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            _, st = fields.forward(nside, S, precision=args.precision, out=out, stream=stream)
+            trace_ms.append(st.trace_ms)
+            kernels += st.kernels
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    clk = clocks.summary()
+    elapsed_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    ms_per_step = elapsed_ms / args.steps
+    ray_steps = npix * S
+    value = world * ray_steps / (ms_per_step * 1e-3)
+    kernel_ms = float(np.mean(trace_ms))
+    achieved = FLOP_PER_RAY_STEP * ray_steps / (kernel_ms * 1e-3)
+
+    result = {"metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world,
+              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else
+              ("f64" if args.precision == "fp64" else "f32/f16"), "data": "synthetic", "config": cfg,
+              "gpu_launches": kernels}
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "trace_traffic.json")
+    if os.path.isfile(prof):
+        try:
+            per = json.load(open(prof)).get("dram_bytes_per_ray_step", {}).get(args.precision)
+            if per is not None:
+                traffic = per * ray_steps
+        except (OSError, ValueError):
+            traffic = None
+    result["roofline"] = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_fp32 / 1e12,
+                          "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": traffic,
+                          "kernel_ms": kernel_ms, "flop_per_ray_step": FLOP_PER_RAY_STEP,
+                          "peak_source": "measured on this GPU by srt_probe_peak (FP32 FMA loop, burst)",
+                          "fp64_peak_tflops": peak_fp64 / 1e12,
+                          "gather_GBps": GATHER_BYTES_PER_RAY_STEP * ray_steps / (kernel_ms * 1e-3) / 1e9}
+    result["clocks"] = clk
+
+    # ---- end to end through the C ABI with host buffers
+    if args.e2e_steps > 0:
+        phi_h = torch.empty(phi_d.shape, dtype=torch.float32, pin_memory=True)
+        b_h = torch.empty(b_d.shape, dtype=torch.float32, pin_memory=True)
+        phi_h.copy_(phi_d)
+        b_h.copy_(b_d)
+        fields.close()
+        del phi_d, b_d
+        torch.cuda.empty_cache()
+        phi_np, b_np = phi_h.numpy(), b_h.numpy()
+        maps_h = np.zeros((6, npix), np.float32)
+        times = []
+        for i in range(args.e2e_steps + 1):
+            barrier(world)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with srt.Fields(phi_np, b_np) as f:
+                f.forward(nside, S, precision=args.precision, out=maps_h)
+            t1 = time.perf_counter()
+            if i > 0:
+                times.append(t1 - t0)
+        e2e_s = max_over_ranks(float(np.mean(times)), world)
+        result["e2e"] = {"value": world * ray_steps / e2e_s, "unit": "ray-steps/s",
+                         "h2d_bytes_per_step": int(phi_np.nbytes + b_np.nbytes),
+                         "d2h_bytes_per_step": int(maps_h.nbytes), "ms_per_step": e2e_s * 1e3}
+        fields = srt.Fields(phi_np, b_np)
+    else:
+        phi_np = b_np = None
+
+    # ---- comparison legs on one batch (rank 0 only)
+    if rank == 0 and args.compare_batch >= 0:
+        b0, cnt = args.compare_batch * nside * nside, nside * nside
+        legs = {}
+        bout = torch.empty((6, cnt), dtype=torch.float32, device=dev)
+        maps = {}
+        for mode in ("mixed", "fp64", "ref16"):
+            fields.forward(nside, S, b0, cnt, precision=mode, out=bout, stream=stream)  # warm (REF16 builds its planes)
+            _, st = fields.forward(nside, S, b0, cnt, precision=mode, out=bout, stream=stream)
+            torch.cuda.synchronize()
+            legs[mode] = {"ray_steps_per_s": cnt * S / (st.trace_ms * 1e-3), "kernel_ms": st.trace_ms}
+            maps[mode] = bout.cpu().numpy()
+        cmp = {"batch": args.compare_batch, "rays": cnt, "legs": legs,
+               "mixed_over_fp64": legs["mixed"]["ray_steps_per_s"] / legs["fp64"]["ray_steps_per_s"],
+               "mixed_over_ref16": legs["mixed"]["ray_steps_per_s"] / legs["ref16"]["ray_steps_per_s"],
+               "mixed_vs_fp64_error": map_errors(maps["mixed"], maps["fp64"]),
+               "ref16_vs_fp64_error": map_errors(maps["ref16"], maps["fp64"])}
+        if phi_np is not None and args.oracle_sample > 0:
+            from oracle import oracle
+
+            pix = sample_pixels(nside, args.oracle_sample, b0, cnt, seed=1)
+            want = oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="fp64")
+            cmp["oracle_sample"] = {"pixels": len(pix),
+                                    "fp64_gpu_vs_oracle": map_errors(maps["fp64"][:, pix - b0], want),
+                                    "mixed_gpu_vs_oracle": map_errors(maps["mixed"][:, pix - b0], want)}
+        result["compare"] = cmp
+
+    # ---- CPU baseline: FP64 oracle on a bounded sample (rank 0, N = 1 only)
+    if rank == 0 and world == 1 and phi_np is not None and args.cpu_seconds > 0:
+        from oracle import oracle
+
+        cores = oracle.max_threads()
+        rays, dt = time_cpu(lambda pix: oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="fp64",
+                                                            threads=cores),
+                            args.cpu_seconds, lambda k: sample_pixels(nside, k, seed=2))
+        result["cpu_baseline"] = {"value": rays * S / dt, "unit": "ray-steps/s", "cores": cores, "kind": "port",
+                                  "sample": "%d random pixels of the same workload x %d steps, FP64 oracle, "
+                                            "%.1f s" % (rays, S, dt)}
+    fields.close()
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------- reference arm
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+
+    import srt_fields
+    from oracle import oracle
+
+    n, nside, S = args.n, args.nside, args.n_steps
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    phi_t, b_t = srt_fields.gaussian_fields_torch(n, seed=args.seed, device=dev)
+    phi_np, b_np = phi_t.cpu().numpy(), b_t.cpu().numpy()
+    del phi_t, b_t
+    use_ref = oracle.ref_available()
+    cores = oracle.max_threads()
+    if use_ref:
+        def run(pix):
+            # the reference's own host code traces contiguous RING ranges
+            oracle.ref_trace(phi_np, b_np, nside, S, int(pix[0]), len(pix), threads=cores)
+        make = lambda k: np.arange(k) + 5 * nside * nside  # noqa: E731
+        kind = "reference"
+    else:
+        def run(pix):
+            oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="ref16", threads=cores)
+        make = lambda k: sample_pixels(nside, k, seed=3)  # noqa: E731
+        kind = "port"
+    per_step_s = max(2.0, min(20.0, 60.0 / max(args.steps + args.warmup, 1)))
+    rays, dt = time_cpu(run, per_step_s, make)
+    pix = make(rays)
+    for _ in range(args.warmup):
+        run(pix)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run(pix)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = rays * S / dt
+    sample = ("%d pixels x %d steps of the %d^3 / nside %d workload per step, %s" %
+              (rays, S, n, nside, "reference host code (oracle/_ref)" if use_ref else
+               "oracle REF16 port of the reference's arithmetic"))
+    res = {"impl": "reference", "metric": "ray-steps/s", "value": value, "unit": "ray-steps/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32/f16", "data": "synthetic",
+           "config": {"workload": "forward trace, %d^3 fields, nside %d, %d steps (CPU, reference arithmetic)"
+                                  % (n, nside, S), "grid": n, "nside": nside, "n_steps": S},
+           "cpu_baseline": {"value": value, "unit": "ray-steps/s", "cores": cores, "kind": kind, "sample": sample},
+           "e2e": {"value": value, "unit": "ray-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "gpu_launches": 0}
+    print(json.dumps(res))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

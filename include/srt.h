@@ -1,0 +1,203 @@
+/*
+ * srt.h — C ABI of the GB300-native snapshot ray tracer (libsrt.so).
+ *
+ * The reference program (snapshot-raytracer.cu) has no library API: its only
+ * boundary is the CLI in main() (snapshot-raytracer.cu:600-1007) and, inside
+ * it, one device launch of raytracing_kernel (snapshot-raytracer.cu:552-583,
+ * launched at :897-901). Each entry point below names the part of that program
+ * it replaces. All functions:
+ *   - return SRT_OK (0) on success and a negative SRT_ERR_* code on failure;
+ *     the message of the last failure on the calling thread is available from
+ *     srt_last_error(); nothing here calls exit();
+ *   - take plain pointers and sizes; "host" pointers are ordinary CPU memory
+ *     (pinned or pageable), "device" pointers are CUDA global memory of the
+ *     current device;
+ *   - are synchronous unless SRT_ASYNC is passed, in which case work is
+ *     ordered on the given cudaStream_t (passed as void*; NULL = legacy
+ *     default stream).
+ * A handle may be used from one thread at a time.
+ *
+ * Grid convention (mirrors snapshot-raytracer.cu:216-256, :560, :645): a
+ * scalar field is a flat array of n0*n1*n2 floats in which voxel (i,j,k)
+ * lives at index i + n0*(j + n1*k); i is the x axis and varies fastest. The
+ * CLI passes the HDF5 extents of /data in file order (dims[0], dims[1],
+ * dims[2]) as (n0, n1, n2), exactly as the reference does, which is only
+ * self-consistent for cubic grids. The grid is periodic; voxel i sits at
+ * coordinate x = i and the observer at (n0/2, n1/2, n2/2).
+ *
+ * Maps (order used everywhere below, the reference's write order,
+ * snapshot-raytracer.cu:941-987):
+ *   0 dA, 1 ellipticity1, 2 ellipticity2, 3 rotation, 4 deflection1,
+ *   5 deflection2.
+ */
+#ifndef SRT_H
+#define SRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SRT_ABI_VERSION 1
+
+/* status codes */
+#define SRT_OK 0
+#define SRT_ERR_INVALID_ARGUMENT (-1)
+#define SRT_ERR_CUDA (-2)
+#define SRT_ERR_OUT_OF_MEMORY (-3)
+#define SRT_ERR_IO (-4)
+#define SRT_ERR_FORMAT (-5)
+#define SRT_ERR_NO_DEVICE (-6)
+#define SRT_ERR_UNSUPPORTED (-7)
+
+/* precision modes of srt_forward / srt_vjp */
+#define SRT_PRECISION_FP64 0  /* all-FP64 interpolation, right-hand side and state */
+#define SRT_PRECISION_MIXED 1 /* FP32 interpolation and right-hand side on a
+                                 perturbation state; FP64 only at ray setup
+                                 and map extraction */
+#define SRT_PRECISION_REF16 2 /* the reference's own arithmetic: B quantised to
+                                 FP16 x 2^27, FP32 interpolation with the cell
+                                 offset taken in FP32, FP64 state */
+
+/* flags */
+#define SRT_INPUT_DEVICE 1u  /* srt_fields_create: phi / b point to device memory */
+#define SRT_OUTPUT_DEVICE 2u /* srt_forward / srt_vjp: outputs are device memory */
+#define SRT_ASYNC 4u         /* do not synchronise; order work on `stream` */
+#define SRT_ACCUMULATE 8u    /* srt_vjp: add into the gradient grids instead of
+                                overwriting them */
+#define SRT_DETERMINISTIC 16u /* srt_vjp: order-independent (bitwise
+                                 reproducible) FP64 gradient accumulation */
+
+#define SRT_NUM_MAPS 6
+
+typedef struct srt_fields srt_fields;
+
+typedef struct srt_stats {
+  double trace_ms;     /* device time of the trace (or adjoint) kernels, CUDA events */
+  double total_ms;     /* host wall time of the call */
+  int64_t rays;        /* rays traced */
+  int64_t ray_steps;   /* rays x n_steps */
+  int64_t kernels;     /* kernels this call launched */
+  int64_t h2d_bytes;   /* bytes copied host -> device by this call */
+  int64_t d2h_bytes;   /* bytes copied device -> host by this call */
+} srt_stats;
+
+/* ---------------------------------------------------------------- library */
+
+/* ABI version (SRT_ABI_VERSION). */
+int srt_abi_version(void);
+
+/* Message of the last failure on this thread ("" if none); returns the
+ * message length. Replaces the reference's std::cerr diagnostics
+ * (snapshot-raytracer.cu:30-186, :602-631, :721-913). */
+int srt_last_error(char* buf, size_t len);
+
+/* Number of CUDA devices visible (0 when there is no GPU; never fails). */
+int srt_device_count(void);
+
+/* --------------------------------------------------------------- fields */
+
+/* Upload (or adopt from device memory) the Weyl potential phi and the shift
+ * vector field B and lay them out for tracing: a periodic halo of one voxel
+ * before and two after on every axis, one FP32 plane per B component.
+ * phi: n0*n1*n2 floats; b_xyz: 3*n0*n1*n2 floats interleaved per voxel
+ * (B_x, B_y, B_z of voxel v at b_xyz[3v+0..2]), the layout of the reference's
+ * HDF5 vector read (snapshot-raytracer.cu:89-186). Host inputs are streamed
+ * in slabs, so peak device memory is the laid-out fields plus one slab.
+ * Replaces snapshot-raytracer.cu:752-855 (cudaMalloc of the fields, the three
+ * staged vector3_to_half passes and the phi copy). */
+int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t n1,
+                      int64_t n2, unsigned flags, void* stream, srt_fields** out);
+
+/* Release the device memory of a fields handle (NULL is a no-op). Replaces
+ * the reference's cudaFree calls (snapshot-raytracer.cu:917-920, :993-998). */
+int srt_fields_destroy(srt_fields* fields);
+
+/* Device bytes held by a fields handle. */
+int64_t srt_fields_bytes(const srt_fields* fields);
+
+/* -------------------------------------------------------------- forward */
+
+/* Trace one ray per HEALPix RING pixel p in [pix_begin, pix_begin+pix_count)
+ * for n_steps RK4 steps of one grid unit and write the six maps:
+ * maps[m][p - pix_begin] (m in the map order above; each maps[m] holds
+ * pix_count floats, on the host unless SRT_OUTPUT_DEVICE).
+ * Rays are set up from the pixel centres and the observer at the box centre on
+ * the device and launched in NESTED order for locality; results are stored at
+ * their RING index. The CLI's batch b is pix_begin = b*nside^2,
+ * pix_count = nside^2 (snapshot-raytracer.cu:708-717); all pixels is
+ * pix_begin = 0, pix_count = 12*nside^2.
+ * Replaces snapshot-raytracer.cu:857-913 (pix2ang loop, theta/phi upload,
+ * raytracing_kernel launch) and the map read-back of :941-987.
+ * Errors: nside < 1 or nside > 2^16, pix range outside [0, 12*nside^2],
+ * n_steps < 1 or > 2^22, unknown precision -> SRT_ERR_INVALID_ARGUMENT. */
+int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
+                int n_steps, int precision, float* const maps[SRT_NUM_MAPS], unsigned flags,
+                void* stream, srt_stats* stats);
+
+/* ------------------------------------------------------------------ vjp */
+
+/* Gradient of L = sum_m sum_p weights[m][p] * maps[m][p] (maps as produced by
+ * srt_forward with the same arguments) with respect to the phi grid and the
+ * three B component grids. dphi: n0*n1*n2 floats; db_xyz: 3*n0*n1*n2 floats
+ * interleaved like the b_xyz input. Either may be NULL to skip it. The forward
+ * state is checkpointed every ckpt_every steps (<= 0 picks ~sqrt(n_steps)) and
+ * each segment is recomputed during the reverse sweep. Gradients are
+ * overwritten unless SRT_ACCUMULATE. SRT_DETERMINISTIC accumulates in 64-bit
+ * fixed point so repeated calls give identical bits.
+ * No counterpart in the reference (it has no derivatives); the forward it
+ * differentiates is snapshot-raytracer.cu:315-583. */
+int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
+            int n_steps, int precision, const float* const weights[SRT_NUM_MAPS], float* dphi,
+            float* db_xyz, int ckpt_every, unsigned flags, void* stream, srt_stats* stats);
+
+/* ---------------------------------------------------------- measurement */
+
+/* Measured FMA issue rate of the current GPU (FLOP/s, one FMA = 2 FLOP):
+ * kind 0 = FP32, kind 1 = FP64. This is the roofline denominator of the trace
+ * kernels, which are bound by CUDA-core issue rather than by a tensor core or
+ * by HBM. No counterpart in the reference. */
+int srt_probe_peak(int kind, double* flops_per_s);
+
+/* ------------------------------------------------------------- HEALPix */
+
+/* RING pixel centre: colatitude theta and longitude phi (radians). Replaces
+ * chealpix pix2ang_ring64 (snapshot-raytracer.cu:865). */
+int srt_pix2ang_ring(int64_t nside, int64_t pix, double* theta, double* phi);
+/* NESTED -> RING and RING -> NESTED pixel index (-1 on bad input). */
+int64_t srt_nest2ring(int64_t nside, int64_t ipnest);
+int64_t srt_ring2nest(int64_t nside, int64_t ipring);
+
+/* ----------------------------------------------------- files (host only) */
+
+/* Read dataset `dset` (e.g. "/data") of an HDF5 file as native float, any
+ * rank. On success *data is malloc'ed (free with srt_free), dims[0..*rank-1]
+ * hold the extents in file order. Replaces load_hdf5_array
+ * (snapshot-raytracer.cu:22-87). */
+int srt_h5_read_scalar(const char* path, const char* dset, float** data, int64_t dims[8],
+                       int* rank);
+/* Read a rank-3 dataset whose element type is array[3] of float (the B
+ * field); *data holds 3*n voxels interleaved. Replaces load_hdf5_vector_field
+ * (snapshot-raytracer.cu:89-186), including its rank and element-type checks. */
+int srt_h5_read_vector3(const char* path, const char* dset, float** data, int64_t dims[3]);
+/* Write a float32 dataset (rank 1..8, dims in file order); vector3 != 0 writes
+ * array[3] of float elements over a rank-3 dataspace (3 floats per element). */
+int srt_h5_write(const char* path, const char* dset, const float* data, const int64_t* dims,
+                 int rank, int vector3);
+/* Write a HEALPix map as a FITS binary table (one float32 column, RING or
+ * NESTED ordering keyword, COORDSYS). Replaces chealpix write_healpix_map
+ * (snapshot-raytracer.cu:947-987). overwrite == 0 refuses to replace an
+ * existing file, as cfitsio does for a plain file name. */
+int srt_fits_write_map(const char* path, const float* map, int64_t nside, int nest,
+                       const char* coordsys, int overwrite);
+/* Read back a map written by srt_fits_write_map (or any single-column float32
+ * HEALPix BINTABLE); *map is malloc'ed (free with srt_free). */
+int srt_fits_read_map(const char* path, float** map, int64_t* npix, int64_t* nside, int* nest);
+void srt_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SRT_H */

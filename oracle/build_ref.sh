@@ -1,0 +1,15 @@
+#!/bin/sh
+# Compile the reference's own host code for the tracer's path into
+# oracle/_ref/libsrt_ref.so (test infrastructure: golden vectors and the pin of
+# the oracle). Reads the reference sources where they lie; writes only into
+# oracle/_ref/. Usage: oracle/build_ref.sh [REFERENCE_DIR]
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+[ -f "$REF/snapshot-raytracer.cu" ] || { echo "reference source not found in $REF" >&2; exit 3; }
+mkdir -p "$HERE/_ref"
+# Reference flags (Makefile:9-10,33): -O3 --use_fast_math -std=c++17 -fopenmp;
+# one Blackwell gencode for its device code, which the library never launches.
+nvcc -O3 --use_fast_math -std=c++17 -shared -Xcompiler -fopenmp,-fPIC,-ffp-contract=off \
+  -gencode arch=compute_103a,code=sm_103a -w \
+  -I"$HERE/stubs" -I"$REF" "$HERE/ref_harness.cu" -o "$HERE/_ref/libsrt_ref.so"

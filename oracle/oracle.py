@@ -1,0 +1,142 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so) and of the
+reference's own host code (oracle/_ref/libsrt_ref.so, only where it was built).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference legs, as the checker or the timed CPU
+baseline — never by the product path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBORACLE = os.path.join(HERE, "liboracle.so")
+LIBREF = os.path.join(HERE, "_ref", "libsrt_ref.so")
+
+MODE = {"fp64": 0, "ref16": 2}
+_P, _I64 = ctypes.c_void_p, ctypes.c_int64
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIBORACLE):
+            raise RuntimeError("oracle not built: %s" % LIBORACLE)
+        L = ctypes.CDLL(LIBORACLE)
+        L.srto_trace.argtypes = [_P, _P, _I64, _I64, _I64, _I64, _I64, _I64, ctypes.c_int, ctypes.c_int, _P,
+                                 ctypes.c_int]
+        L.srto_trace_pixels.argtypes = [_P, _P, _I64, _I64, _I64, _I64, _P, _I64, ctypes.c_int, ctypes.c_int, _P,
+                                        ctypes.c_int]
+        L.srto_pix2ang_ring.argtypes = [_I64, _I64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.srto_pix2ang_ring.restype = None
+        L.srto_interp.argtypes = [_P, _P, _I64, _I64, _I64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_double, _P]
+        L.srto_float_to_half.argtypes = [ctypes.c_float]
+        L.srto_float_to_half.restype = ctypes.c_uint16
+        L.srto_half_to_float.argtypes = [ctypes.c_uint16]
+        L.srto_half_to_float.restype = ctypes.c_float
+        L.srto_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def ref_available():
+    return os.path.isfile(LIBREF)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("reference host library not built (needs the reference sources): %s" % LIBREF)
+        L = ctypes.CDLL(LIBREF)
+        L.srtref_trace_angles.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _I64, ctypes.c_int,
+                                          _P, ctypes.c_int]
+        L.srtref_interp.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, _P]
+        _ref = L
+    return _ref
+
+
+def _dims(phi, b):
+    phi = np.ascontiguousarray(phi, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    n2, n1, n0 = phi.shape
+    assert b.shape == (n2, n1, n0, 3)
+    return phi, b, n0, n1, n2
+
+
+def max_threads():
+    return lib().srto_max_threads()
+
+
+def trace(phi, b, nside, n_steps, pix_begin=0, pix_count=None, mode="fp64", threads=0):
+    """(6, count) maps of RING pixels [pix_begin, pix_begin + count)."""
+    phi, b, n0, n1, n2 = _dims(phi, b)
+    if pix_count is None:
+        pix_count = 12 * nside * nside - pix_begin
+    out = np.zeros((6, pix_count), np.float32)
+    rc = lib().srto_trace(phi.ctypes.data, b.ctypes.data, n0, n1, n2, nside, pix_begin, pix_count, n_steps,
+                          MODE[mode], out.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError("srto_trace failed (%d)" % rc)
+    return out
+
+
+def trace_pixels(phi, b, nside, n_steps, pixels, mode="fp64", threads=0):
+    """(6, len(pixels)) maps of an arbitrary list of RING pixels."""
+    phi, b, n0, n1, n2 = _dims(phi, b)
+    pix = np.ascontiguousarray(pixels, np.int64)
+    out = np.zeros((6, len(pix)), np.float32)
+    rc = lib().srto_trace_pixels(phi.ctypes.data, b.ctypes.data, n0, n1, n2, nside, pix.ctypes.data, len(pix),
+                                 n_steps, MODE[mode], out.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError("srto_trace_pixels failed (%d)" % rc)
+    return out
+
+
+def pix2ang_ring(nside, pix):
+    t, p = ctypes.c_double(), ctypes.c_double()
+    lib().srto_pix2ang_ring(nside, pix, ctypes.byref(t), ctypes.byref(p))
+    return t.value, p.value
+
+
+def interp(phi, b, field, x, y, z, mode="fp64"):
+    phi, b, n0, n1, n2 = _dims(phi, b)
+    out = np.zeros(10, np.float64)
+    lib().srto_interp(phi.ctypes.data, b.ctypes.data, n0, n1, n2, MODE[mode], field, x, y, z, out.ctypes.data)
+    return out
+
+
+def float_to_half_bits(x):
+    return lib().srto_float_to_half(float(x))
+
+
+def half_bits_to_float(h):
+    return lib().srto_half_to_float(int(h))
+
+
+def ref_trace(phi, b, nside, n_steps, pix_begin=0, pix_count=None, threads=0):
+    """The reference's own host code (oracle/_ref) on RING pixels
+    [pix_begin, pix_begin + count), ray angles from the oracle's pix2ang."""
+    phi, b, n0, n1, n2 = _dims(phi, b)
+    if pix_count is None:
+        pix_count = 12 * nside * nside - pix_begin
+    th = np.zeros(pix_count)
+    ph = np.zeros(pix_count)
+    for i in range(pix_count):
+        th[i], ph[i] = pix2ang_ring(nside, pix_begin + i)
+    out = np.zeros((6, pix_count), np.float32)
+    ref_lib().srtref_trace_angles(phi.ctypes.data, b.ctypes.data, n0, n1, n2, th.ctypes.data, ph.ctypes.data,
+                                  pix_count, n_steps, out.ctypes.data, threads)
+    return out
+
+
+def ref_interp(phi, b, field, x, y, z):
+    phi, b, n0, n1, n2 = _dims(phi, b)
+    out = np.zeros(10, np.float64)
+    ref_lib().srtref_interp(phi.ctypes.data, b.ctypes.data, n0, n1, n2, field, x, y, z, out.ctypes.data)
+    return out

@@ -1,0 +1,105 @@
+"""Build recipe of the tracer: libsrt.so (CUDA kernels for sm_103a + C ABI +
+host file formats), the `snapshot-raytracer` CLI, and the CPU oracle used by
+the tests (oracle/liboracle.so, plus oracle/_ref/libsrt_ref.so when the
+reference sources are present on this machine).
+
+Everything is built in-tree with explicit nvcc / g++ / gcc commands, compiled
+in parallel. Usage: python snapshot-raytracer_gb300/build_srt.py [-v]
+"""
+import concurrent.futures
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIBDIR = os.path.join(PKG, "lib")
+LIBSRT = os.path.join(LIBDIR, "libsrt.so")
+CLI = os.path.join(PKG, "snapshot-raytracer")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIBORACLE = os.path.join(ORACLE_DIR, "liboracle.so")
+REFERENCE_DIR = os.environ.get("SRT_REFERENCE_DIR", "/root/reference")
+LIBREF = os.path.join(ORACLE_DIR, "_ref", "libsrt_ref.so")
+
+GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC = os.environ.get("NVCC", "nvcc")
+CUDA_SOURCES = ["srt_kernels.cu", "srt_adjoint.cu", "srt_api.cu"]
+HOST_SOURCES = ["srt_io.cpp"]
+
+
+def _run(cmd, verbose):
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed (%d): %s\n%s" % (r.returncode, " ".join(cmd), r.stdout))
+    if verbose and r.stdout.strip():
+        print(r.stdout, flush=True)
+    return r.stdout
+
+
+def _nvcc_obj(src, verbose):
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    cmd = [NVCC, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-c", src, "-o", obj]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    _run(cmd, verbose)
+    return obj
+
+
+def _gxx_obj(src, verbose):
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    cuda_home = os.path.dirname(os.path.dirname(shutil.which(NVCC) or "/usr/local/cuda/bin/nvcc"))
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
+           "-I" + os.path.join(cuda_home, "include"), "-c", src, "-o", obj]
+    _run(cmd, verbose)
+    return obj
+
+
+def build_oracle(verbose=False):
+    """The CPU oracle (test infrastructure)."""
+    _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+          "-o", LIBORACLE, os.path.join(ORACLE_DIR, "srt_oracle.c"), "-lm"], verbose)
+    return LIBORACLE
+
+
+def build_reference(verbose=False):
+    """The reference's own host code for the path (only where its sources exist)."""
+    if not os.path.isfile(os.path.join(REFERENCE_DIR, "snapshot-raytracer.cu")):
+        return None
+    _run(["sh", os.path.join(ORACLE_DIR, "build_ref.sh"), REFERENCE_DIR], verbose)
+    return LIBREF
+
+
+def build(verbose=False, oracle=True, reference=True):
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    jobs = []
+    with concurrent.futures.ThreadPoolExecutor(max_workers=8) as ex:
+        for s in CUDA_SOURCES:
+            jobs.append(ex.submit(_nvcc_obj, os.path.join(CSRC, s), verbose))
+        for s in HOST_SOURCES:
+            jobs.append(ex.submit(_gxx_obj, os.path.join(CSRC, s), verbose))
+        side = []
+        if oracle:
+            side.append(ex.submit(build_oracle, verbose))
+        if reference:
+            side.append(ex.submit(build_reference, verbose))
+        objs = [j.result() for j in jobs]
+        _run([NVCC, *GENCODE, "-shared", "-o", LIBSRT, *objs], verbose)
+        cli_src = os.path.join(CSRC, "srt_cli.cpp")
+        if os.path.isfile(cli_src):
+            _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), cli_src, "-o", CLI,
+                  "-L" + LIBDIR, "-lsrt", "-Wl,-rpath,$ORIGIN/lib"], verbose)
+        for j in side:
+            j.result()
+    return LIBSRT
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print("built", LIBSRT)

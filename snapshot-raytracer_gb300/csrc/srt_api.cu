@@ -1,0 +1,323 @@
+// srt_api.cu — the C ABI of libsrt (declared in include/srt.h): field upload
+// and layout, the forward trace, HEALPix helpers and error reporting.
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include "srt_internal.h"
+
+namespace {
+thread_local std::string g_last_error;
+
+struct HostTimer {
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  double ms() const {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+// Largest slab of a host field staged on the device at a time.
+constexpr int64_t kSlabBytes = 512ll << 20;
+
+bool dims_ok(int64_t n0, int64_t n1, int64_t n2) {
+  const int64_t lim = int64_t(1) << 20;
+  if (n0 < 1 || n1 < 1 || n2 < 1 || n0 > lim || n1 > lim || n2 > lim) return false;
+  // positions and cell indices are kept in 32-bit integers / FP32 on the mixed path
+  return true;
+}
+}  // namespace
+
+namespace srt {
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation)
+    return set_error(SRT_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return set_error(SRT_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+  return set_error(SRT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+Geom make_geom(const srt_fields* f) {
+  Geom g;
+  for (int i = 0; i < 3; ++i) {
+    g.n[i] = (int)f->n[i];
+    g.invn[i] = 1.0f / (float)f->n[i];
+  }
+  g.px = f->pn[0];
+  g.pxy = f->pn[0] * f->pn[1];
+  return g;
+}
+
+FieldPtrs make_ptrs(const srt_fields* f) {
+  FieldPtrs p;
+  p.phi = f->phi;
+  for (int c = 0; c < 3; ++c) {
+    p.b[c] = f->b[c];
+    p.bh[c] = f->bh[c];
+  }
+  return p;
+}
+
+}  // namespace srt
+
+using namespace srt;
+
+#define SRT_CUDA_TRY(expr, what)                 \
+  do {                                           \
+    cudaError_t _e = (expr);                     \
+    if (_e != cudaSuccess) {                     \
+      rc = cuda_error(_e, what);                 \
+      goto fail;                                 \
+    }                                            \
+  } while (0)
+
+extern "C" {
+
+int srt_abi_version(void) { return SRT_ABI_VERSION; }
+
+int srt_last_error(char* buf, size_t len) {
+  if (buf && len > 0) {
+    strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = '\0';
+  }
+  return (int)g_last_error.size();
+}
+
+int srt_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t n1, int64_t n2,
+                      unsigned flags, void* stream, srt_fields** out) {
+  if (!out) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_create: out is NULL");
+  *out = nullptr;
+  if (!phi || !b_xyz) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_create: phi and b_xyz are required");
+  if (!dims_ok(n0, n1, n2))
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_create: bad grid extents %lld x %lld x %lld",
+                     (long long)n0, (long long)n1, (long long)n2);
+  if (srt_device_count() < 1) return set_error(SRT_ERR_NO_DEVICE, "srt_fields_create: no CUDA device");
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool dev_in = (flags & SRT_INPUT_DEVICE) != 0;
+  int rc = SRT_OK;
+  float* slab = nullptr;
+  srt_fields* f = new (std::nothrow) srt_fields();
+  if (!f) return set_error(SRT_ERR_OUT_OF_MEMORY, "srt_fields_create: host allocation failed");
+  {
+    cudaGetDevice(&f->device);
+    for (int i = 0; i < 3; ++i) {
+      f->n[i] = (i == 0 ? n0 : (i == 1 ? n1 : n2));
+      f->pn[i] = f->n[i] + 3;
+    }
+    const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
+    const int64_t plane = n0 * n1;
+    SRT_CUDA_TRY(cudaMalloc(&f->phi, pvox * sizeof(float)), "cudaMalloc(phi)");
+    for (int c = 0; c < 3; ++c) SRT_CUDA_TRY(cudaMalloc(&f->b[c], pvox * sizeof(float)), "cudaMalloc(B)");
+    f->bytes = 4 * pvox * (int64_t)sizeof(float);
+    if (dev_in) {
+      SRT_CUDA_TRY(launch_pad_slab(phi, 1, 0, f->phi, f->n, f->pn, 0, n2, s), "pad phi");
+      for (int c = 0; c < 3; ++c)
+        SRT_CUDA_TRY(launch_pad_slab(b_xyz, 3, c, f->b[c], f->n, f->pn, 0, n2, s), "pad B");
+    } else {
+      // stream host planes through one device slab
+      int64_t kslab = kSlabBytes / (plane * 3 * (int64_t)sizeof(float));
+      if (kslab < 1) kslab = 1;
+      if (kslab > n2) kslab = n2;
+      SRT_CUDA_TRY(cudaMalloc(&slab, kslab * plane * 3 * sizeof(float)), "cudaMalloc(slab)");
+      for (int64_t k0 = 0; k0 < n2; k0 += kslab) {
+        const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
+        SRT_CUDA_TRY(cudaMemcpyAsync(slab, phi + k0 * plane, (k1 - k0) * plane * sizeof(float),
+                                     cudaMemcpyHostToDevice, s),
+                     "copy phi slab");
+        SRT_CUDA_TRY(launch_pad_slab(slab, 1, 0, f->phi, f->n, f->pn, k0, k1, s), "pad phi");
+      }
+      for (int64_t k0 = 0; k0 < n2; k0 += kslab) {
+        const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
+        SRT_CUDA_TRY(cudaMemcpyAsync(slab, b_xyz + 3 * k0 * plane, 3 * (k1 - k0) * plane * sizeof(float),
+                                     cudaMemcpyHostToDevice, s),
+                     "copy B slab");
+        for (int c = 0; c < 3; ++c)
+          SRT_CUDA_TRY(launch_pad_slab(slab, 3, c, f->b[c], f->n, f->pn, k0, k1, s), "pad B");
+      }
+    }
+    if (!(flags & SRT_ASYNC) || slab) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
+    if (slab) cudaFree(slab);
+    slab = nullptr;
+  }
+  *out = f;
+  return SRT_OK;
+fail:
+  if (slab) cudaFree(slab);
+  srt_fields_destroy(f);
+  return rc;
+}
+
+int srt_fields_destroy(srt_fields* f) {
+  if (!f) return SRT_OK;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (prev != f->device) cudaSetDevice(f->device);
+  cudaFree(f->phi);
+  for (int c = 0; c < 3; ++c) {
+    cudaFree(f->b[c]);
+    cudaFree(f->bh[c]);
+  }
+  if (prev != f->device) cudaSetDevice(prev);
+  delete f;
+  return SRT_OK;
+}
+
+int64_t srt_fields_bytes(const srt_fields* f) { return f ? f->bytes : 0; }
+
+int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
+                int precision, float* const maps[SRT_NUM_MAPS], unsigned flags, void* stream,
+                srt_stats* stats) {
+  HostTimer wall;
+  if (!fields) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: fields is NULL");
+  if (nside < 1 || nside > (int64_t(1) << 16))
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: invalid nside %lld", (long long)nside);
+  const int64_t npix = 12 * nside * nside;
+  if (pix_begin < 0 || pix_count < 0 || pix_begin > npix || pix_count > npix - pix_begin)
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: pixel range [%lld, %lld) outside [0, %lld)",
+                     (long long)pix_begin, (long long)(pix_begin + pix_count), (long long)npix);
+  if (n_steps < 1 || n_steps > (1 << 22))
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: invalid n_steps %d", n_steps);
+  if (precision != SRT_PRECISION_FP64 && precision != SRT_PRECISION_MIXED && precision != SRT_PRECISION_REF16)
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: unknown precision %d", precision);
+  if (!maps) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: maps is NULL");
+  for (int m = 0; m < SRT_NUM_MAPS; ++m)
+    if (!maps[m] && pix_count > 0) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: maps[%d] is NULL", m);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (pix_count == 0) return SRT_OK;
+
+  srt_fields* f = const_cast<srt_fields*>(fields);
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool dev_out = (flags & SRT_OUTPUT_DEVICE) != 0;
+  int rc = SRT_OK;
+  float* dmaps = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int64_t kernels = 0;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (prev != f->device) cudaSetDevice(f->device);
+  {
+    if (precision == SRT_PRECISION_REF16 && !(f->bh[0] && f->bh[1] && f->bh[2])) {
+      // half(B * 2^27) planes for the reference arithmetic, made once per handle
+      const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
+      __half* h[3] = {nullptr, nullptr, nullptr};
+      cudaError_t e = cudaSuccess;
+      for (int c = 0; c < 3 && e == cudaSuccess; ++c) e = cudaMalloc(&h[c], pvox * sizeof(__half));
+      for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+        e = launch_quantize_half(f->b[c], h[c], pvox, s);
+        ++kernels;
+      }
+      if (e != cudaSuccess) {
+        for (int c = 0; c < 3; ++c) cudaFree(h[c]);
+        rc = cuda_error(e, "REF16 B planes");
+        goto fail;
+      }
+      for (int c = 0; c < 3; ++c) f->bh[c] = h[c];
+      f->bytes += 3 * pvox * (int64_t)sizeof(__half);
+    }
+    TraceArgs a;
+    a.F = make_ptrs(f);
+    a.G = make_geom(f);
+    a.nside = nside;
+    int l = 0;
+    while ((int64_t(1) << l) < nside) ++l;
+    a.log2p = l;
+    a.launch_rays = 12 * (int64_t(1) << (2 * l));
+    a.pix_begin = pix_begin;
+    a.pix_count = pix_count;
+    a.n_steps = n_steps;
+    if (dev_out) {
+      for (int m = 0; m < 6; ++m) a.maps[m] = maps[m];
+    } else {
+      SRT_CUDA_TRY(cudaMalloc(&dmaps, 6 * pix_count * sizeof(float)), "cudaMalloc(maps)");
+      for (int m = 0; m < 6; ++m) a.maps[m] = dmaps + m * pix_count;
+    }
+    const bool timed = !(flags & SRT_ASYNC);
+    if (timed) {
+      SRT_CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+      SRT_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+      SRT_CUDA_TRY(cudaEventRecord(e0, s), "cudaEventRecord");
+    }
+    SRT_CUDA_TRY(launch_trace(precision, a, s, &kernels), "trace kernel launch");
+    if (timed) SRT_CUDA_TRY(cudaEventRecord(e1, s), "cudaEventRecord");
+    if (!dev_out) {
+      for (int m = 0; m < 6; ++m)
+        SRT_CUDA_TRY(cudaMemcpyAsync(maps[m], a.maps[m], pix_count * sizeof(float), cudaMemcpyDeviceToHost, s),
+                     "copy maps to host");
+    }
+    if (timed || !dev_out) SRT_CUDA_TRY(cudaStreamSynchronize(s), "trace");
+    if (stats) {
+      float ms = -1.f;
+      if (timed) cudaEventElapsedTime(&ms, e0, e1);
+      stats->trace_ms = ms;
+      stats->rays = pix_count;
+      stats->ray_steps = pix_count * (int64_t)n_steps;
+      stats->kernels = kernels;
+      stats->d2h_bytes = dev_out ? 0 : 6 * pix_count * (int64_t)sizeof(float);
+    }
+  }
+fail:
+  if (dmaps) cudaFree(dmaps);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (prev != f->device) cudaSetDevice(prev);
+  if (stats) stats->total_ms = wall.ms();
+  return rc;
+}
+
+int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
+            int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz, int ckpt_every,
+            unsigned flags, void* stream, srt_stats* stats) {
+  (void)fields; (void)nside; (void)pix_begin; (void)pix_count; (void)n_steps; (void)precision; (void)weights;
+  (void)dphi; (void)db_xyz; (void)ckpt_every; (void)flags; (void)stream; (void)stats;
+  return set_error(SRT_ERR_UNSUPPORTED, "srt_vjp: not available in this build");
+}
+
+int srt_pix2ang_ring(int64_t nside, int64_t pix, double* theta, double* phi) {
+  if (nside < 1 || nside > (int64_t(1) << 29) || pix < 0 || pix >= 12 * nside * nside || !theta || !phi)
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_pix2ang_ring: bad arguments");
+  hp_pix2ang_ring(nside, pix, theta, phi);
+  return SRT_OK;
+}
+
+int64_t srt_nest2ring(int64_t nside, int64_t ipnest) {
+  if (!hp_is_pow2(nside) || nside > (int64_t(1) << 29) || ipnest < 0 || ipnest >= 12 * nside * nside) return -1;
+  return hp_nest2ring(nside, ipnest);
+}
+
+int64_t srt_ring2nest(int64_t nside, int64_t ipring) {
+  if (!hp_is_pow2(nside) || nside > (int64_t(1) << 29) || ipring < 0 || ipring >= 12 * nside * nside) return -1;
+  return hp_ring2nest(nside, ipring);
+}
+
+int srt_probe_peak(int kind, double* flops_per_s) {
+  if (!flops_per_s || (kind != 0 && kind != 1)) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_probe_peak: bad arguments");
+  if (srt_device_count() < 1) return set_error(SRT_ERR_NO_DEVICE, "srt_probe_peak: no CUDA device");
+  cudaError_t e = probe_fma(kind, flops_per_s);
+  if (e != cudaSuccess) return cuda_error(e, "srt_probe_peak");
+  return SRT_OK;
+}
+
+void srt_free(void* p) { free(p); }
+
+}  // extern "C"

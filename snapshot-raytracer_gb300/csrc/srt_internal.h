@@ -1,0 +1,52 @@
+// srt_internal.h — shared declarations between the libsrt translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include <string>
+#include "srt.h"
+#include "srt_scheme.cuh"
+
+// Device memory of one set of laid-out fields (see srt_fields_create).
+struct srt_fields {
+  int device = 0;
+  int64_t n[3] = {0, 0, 0};
+  int64_t pn[3] = {0, 0, 0};  // padded extents n + 3
+  float* phi = nullptr;       // padded FP32 planes
+  float* b[3] = {nullptr, nullptr, nullptr};
+  __half* bh[3] = {nullptr, nullptr, nullptr};  // padded half(B * 2^27), made on first REF16 use
+  int64_t bytes = 0;
+};
+
+namespace srt {
+
+// Error reporting (thread-local last error message).
+int set_error(int code, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+struct TraceArgs {
+  FieldPtrs F;
+  Geom G;
+  int64_t nside;
+  int log2p;           // launch order: Morton over a 2^log2p square per face
+  int64_t launch_rays; // 12 * 4^log2p
+  int64_t pix_begin, pix_count;
+  int n_steps;
+  float* maps[6];
+};
+
+Geom make_geom(const srt_fields* f);
+FieldPtrs make_ptrs(const srt_fields* f);
+
+// Field layout kernels.
+cudaError_t launch_pad_slab(const float* src, int comps, int comp, float* dst, const int64_t n[3],
+                            const int64_t pn[3], int64_t k0, int64_t k1, cudaStream_t s);
+cudaError_t launch_quantize_half(const float* src, __half* dst, int64_t count, cudaStream_t s);
+
+// Trace kernel launch (mode = kFP64 / kMIXED / kREF16).
+cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* kernels);
+
+// Peak issue-rate probes (FMA loop kernels); returns achieved FLOP/s.
+cudaError_t probe_fma(int kind, double* flops_per_s);
+
+}  // namespace srt

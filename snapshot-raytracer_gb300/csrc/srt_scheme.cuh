@@ -1,0 +1,608 @@
+// srt_scheme.cuh — per-ray scheme of the tracer: tricubic Catmull-Rom
+// interpolation with gradient and Hessian, the 19-component geodesic +
+// Jacobi-map right-hand side, fixed-step RK4 and the map extraction.
+//
+// Scheme followed (snapshot-raytracer.cu):
+//   * 1-D Catmull-Rom value / d/dt / d2/dt2 on four taps       :195-212
+//   * separable tricubic pass x -> y -> z, x fastest in memory, :214-312
+//     periodic grid, cell ix = floor(x), taps ix-1 .. ix+2
+//   * right-hand side (normalised n, e1, e2; staggered B with   :315-510
+//     B_x at x-1/2, B_y at y-1/2, B_z at z-1/2; Sachs optical
+//     equations; ellipticity and rotation only while dA > 1/2)
+//   * classic RK4, h = 1 grid unit                              :513-550
+//   * initial state from (theta, phi), extraction of the six    :552-583
+//     maps (deflection projected on e_theta and on -e_phi)
+// The computation is restated here for the GPU (it is not the reference's
+// code): one set of Catmull-Rom weights per axis is formed once per
+// interpolation and reused for all 16 x-runs, the passes are streamed over z
+// so only ten accumulators stay live, the B contributions are accumulated in a
+// loop over components, and fields are read from a halo-padded layout so no
+// tap needs a modulo.
+//
+// Precision modes (SRT_PRECISION_* in srt.h):
+//   FP64  — everything in double.
+//   REF16 — the reference's arithmetic: B planes hold half(B * 2^27), the
+//           interpolation is FP32 with the cell offset taken as
+//           float(x) - float(floor(x)), intermediates of the right-hand side
+//           that the reference keeps in float are float, state is double.
+//   MIXED — FP32 interpolation and right-hand side on a perturbation state
+//           delta = y - y0(s), where y0(s) is the exact solution for
+//           Phi = B = 0 (a straight ray: x = x0 - s n0, n = n0, e = e0,
+//           dA = s, dA' = -1). RK4 is affine, so integrating delta with the
+//           perturbation right-hand side f(y0 + delta) - f(y0) gives the same
+//           iterates as integrating y. Every FP32 quantity is then small and
+//           carries full relative precision; the ray position used to pick
+//           the cell is x0 - s n0 + delta_x with s*n0 split exactly (FMA), and
+//           the state is accumulated with compensated (two-sum) additions.
+//           FP64 is used only for ray setup and map extraction.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+#include <cuda_fp16.h>
+#include "srt_healpix.cuh"
+
+namespace srt {
+
+enum { kFP64 = 0, kMIXED = 1, kREF16 = 2 };
+
+#if defined(__CUDA_ARCH__)
+template <typename T>
+SRT_HD T ldg(const T* p) { return __ldg(p); }
+#else
+template <typename T>
+SRT_HD T ldg(const T* p) { return *p; }
+#endif
+
+// Halo-padded periodic grid: voxel (i,j,k), -1 <= i <= n0+1 (etc.), lives at
+// (i+1) + px*((j+1) + py*(k+1)), px = n0+3, py = n1+3, pxy = px*py.
+struct Geom {
+  int n[3];
+  int64_t px, pxy;
+  float invn[3];
+};
+
+struct FieldPtrs {
+  const float* phi;     // padded FP32
+  const float* b[3];    // padded FP32 B components
+  const __half* bh[3];  // padded half(B * 2^27) (REF16 only)
+};
+
+template <typename T>
+struct Tri {  // value, gradient, Hessian (xx, xy, xz, yy, yz, zz)
+  T v, g[3], h[6];
+};
+
+template <typename T>
+struct CRW {  // Catmull-Rom weights of the 4 taps for value, d/dt, d2/dt2
+  T w[4], g[4], h[4];
+};
+
+// Weights of f(t) = sum_i w_i(t) p_i for the Catmull-Rom cubic through p0..p3
+// on [p1, p2] (tangents (p2 - p0)/2 and (p3 - p1)/2), and of f', f''.
+template <typename T>
+SRT_HD void cr_weights(T t, CRW<T>& c) {
+  const T t2 = t * t, t3 = t2 * t;
+  c.w[0] = T(0.5) * (T(2) * t2 - t - t3);
+  c.w[1] = T(0.5) * (T(3) * t3 - T(5) * t2 + T(2));
+  c.w[2] = T(0.5) * (T(4) * t2 + t - T(3) * t3);
+  c.w[3] = T(0.5) * (t3 - t2);
+  c.g[0] = T(0.5) * (T(4) * t - T(3) * t2 - T(1));
+  c.g[1] = T(0.5) * (T(9) * t2 - T(10) * t);
+  c.g[2] = T(0.5) * (T(8) * t - T(9) * t2 + T(1));
+  c.g[3] = T(0.5) * (T(3) * t2 - T(2) * t);
+  c.h[0] = T(2) - T(3) * t;
+  c.h[1] = T(9) * t - T(5);
+  c.h[2] = T(4) - T(9) * t;
+  c.h[3] = T(3) * t - T(1);
+}
+
+template <typename T>
+SRT_HD T tapv(float x) { return (T)x; }
+template <typename T>
+SRT_HD T tapv(__half x) { return (T)__half2float(x); }
+
+// Tricubic value/gradient/Hessian from the 4x4x4 taps starting at padded
+// index `base` (= the voxel (cx-1, cy-1, cz-1) of cell (cx, cy, cz)).
+template <typename T, typename TapT>
+SRT_HD void tricubic(const TapT* __restrict__ f, int64_t base, int64_t px, int64_t pxy,
+                     const CRW<T>& X, const CRW<T>& Y, const CRW<T>& Z, Tri<T>& r) {
+  T v = 0, g0 = 0, g1 = 0, g2 = 0, h00 = 0, h01 = 0, h02 = 0, h11 = 0, h12 = 0, h22 = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    T a = 0, ay = 0, ayy = 0, ax = 0, axy = 0, axx = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const TapT* row = f + base + c * pxy + b * px;
+      const T p0 = tapv<T>(ldg(row + 0)), p1 = tapv<T>(ldg(row + 1));
+      const T p2 = tapv<T>(ldg(row + 2)), p3 = tapv<T>(ldg(row + 3));
+      const T rv = X.w[0] * p0 + X.w[1] * p1 + X.w[2] * p2 + X.w[3] * p3;
+      const T rx = X.g[0] * p0 + X.g[1] * p1 + X.g[2] * p2 + X.g[3] * p3;
+      const T rxx = X.h[0] * p0 + X.h[1] * p1 + X.h[2] * p2 + X.h[3] * p3;
+      a += Y.w[b] * rv;
+      ay += Y.g[b] * rv;
+      ayy += Y.h[b] * rv;
+      ax += Y.w[b] * rx;
+      axy += Y.g[b] * rx;
+      axx += Y.w[b] * rxx;
+    }
+    v += Z.w[c] * a;
+    g0 += Z.w[c] * ax;
+    g1 += Z.w[c] * ay;
+    g2 += Z.g[c] * a;
+    h00 += Z.w[c] * axx;
+    h01 += Z.w[c] * axy;
+    h02 += Z.g[c] * ax;
+    h11 += Z.w[c] * ayy;
+    h12 += Z.g[c] * ay;
+    h22 += Z.h[c] * a;
+  }
+  r.v = v;
+  r.g[0] = g0;
+  r.g[1] = g1;
+  r.g[2] = g2;
+  r.h[0] = h00;
+  r.h[1] = h01;
+  r.h[2] = h02;
+  r.h[3] = h11;
+  r.h[4] = h12;
+  r.h[5] = h22;
+}
+
+template <typename T>
+SRT_HD void tri_scale(Tri<T>& r, T s) {
+  r.v *= s;
+  for (int i = 0; i < 3; ++i) r.g[i] *= s;
+  for (int i = 0; i < 6; ++i) r.h[i] *= s;
+}
+
+// ------------------------------------------------------------ cell lookup
+
+SRT_HD int wrap64(int64_t c, int n) {
+  int64_t r = c % n;
+  if (r < 0) r += n;
+  return (int)r;
+}
+
+// c mod n in [0, n): a float reciprocal for |c| < 2^24 (every finite ray
+// position), an integer modulo for anything else (e.g. a position made
+// non-finite by non-finite field values), so the result is always in range.
+SRT_HD int wrap32(int c, int n, float invn) {
+  const int q = (int)floorf((float)c * invn);
+  int r = c - q * n;
+  if (r < 0) r += n;
+  if (r >= n) r -= n;
+  if (r < 0 || r >= n) {
+    r = c % n;
+    if (r < 0) r += n;
+  }
+  return r;
+}
+
+SRT_HD int64_t cell_base(const Geom& G, int cx, int cy, int cz) {
+  return (int64_t)cx + G.px * (int64_t)cy + G.pxy * (int64_t)cz;
+}
+
+// FP64 / REF16 interpolation of one field at a double-precision position.
+// IT is the arithmetic type (double for FP64, float for REF16); in REF16 the
+// cell offset is float(x) - float(floor(x)) (snapshot-raytracer.cu:223-230).
+template <typename IT, typename TapT>
+SRT_HD void interp_std(const TapT* f, const Geom& G, double x, double y, double z, Tri<IT>& r) {
+  const double fx = floor(x), fy = floor(y), fz = floor(z);
+  const int64_t ix = (int64_t)fx, iy = (int64_t)fy, iz = (int64_t)fz;
+  IT tx, ty, tz;
+  if (sizeof(IT) == sizeof(float)) {
+    tx = (IT)((float)x - (float)ix);
+    ty = (IT)((float)y - (float)iy);
+    tz = (IT)((float)z - (float)iz);
+  } else {
+    tx = (IT)(x - fx);
+    ty = (IT)(y - fy);
+    tz = (IT)(z - fz);
+  }
+  CRW<IT> X, Y, Z;
+  cr_weights(tx, X);
+  cr_weights(ty, Y);
+  cr_weights(tz, Z);
+  const int64_t base = cell_base(G, wrap64(ix, G.n[0]), wrap64(iy, G.n[1]), wrap64(iz, G.n[2]));
+  tricubic<IT, TapT>(f, base, G.px, G.pxy, X, Y, Z, r);
+}
+
+// --------------------------------------------- right-hand side, FP64 / REF16
+
+// 19-component right-hand side on the full state y (FP64 or REF16 arithmetic).
+// State: 0-2 x, 3-5 n, 6-8 e1, 9-11 e2, 12 dA, 13 dA', 14-15 sigma1/2,
+// 16-17 ellipticity1/2, 18 rotation (snapshot-raytracer.cu:317-335).
+template <int MODE>
+SRT_HD void rhs_std(const double* y, double* dy, const FieldPtrs& F, const Geom& G) {
+  typedef typename std::conditional<MODE == kREF16, float, double>::type IT;
+  double n[3], a[3], b[3];
+  {
+    const double rn = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+    const double ra = sqrt(y[6] * y[6] + y[7] * y[7] + y[8] * y[8]);
+    const double rb = sqrt(y[9] * y[9] + y[10] * y[10] + y[11] * y[11]);
+    for (int i = 0; i < 3; ++i) {
+      n[i] = y[3 + i] / rn;
+      a[i] = y[6 + i] / ra;
+      b[i] = y[9 + i] / rb;
+    }
+  }
+  // B contributions (snapshot-raytracer.cu:377-460): n.grad B, the e.n.grad B
+  // scalars, the tidal matrix and n . Laplacian B; the e_i.grad B vectors the
+  // reference also forms there are never used and are not computed.
+  IT bval[3], ngB[3] = {0, 0, 0}, e1ngB = 0, e2ngB = 0, nlap = 0;
+  IT T[6] = {0, 0, 0, 0, 0, 0};  // xx, xy, xz, yy, yz, zz
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    const double off[3] = {c == 0 ? 0.5 : 0.0, c == 1 ? 0.5 : 0.0, c == 2 ? 0.5 : 0.0};
+    Tri<IT> r;
+    if (MODE == kREF16) {
+      interp_std<IT, __half>(F.bh[c], G, y[0] - off[0], y[1] - off[1], y[2] - off[2], r);
+      tri_scale(r, (IT)(1.0 / 134217728.0));  // taps hold B * 2^27
+    } else {
+      interp_std<IT, float>(F.b[c], G, y[0] - off[0], y[1] - off[1], y[2] - off[2], r);
+    }
+    bval[c] = r.v;
+    for (int i = 0; i < 3; ++i) ngB[i] = (IT)(ngB[i] + r.g[i] * n[c]);
+    const double gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
+    const double ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
+    const double gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
+    e1ngB = (IT)(e1ngB + 0.5 * a[c] * gn + 0.5 * n[c] * ga);
+    e2ngB = (IT)(e2ngB + 0.5 * b[c] * gn + 0.5 * n[c] * gb);
+    // H n for this component's Hessian (rows of the symmetric matrix)
+    const double Hn0 = r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2];
+    const double Hn1 = r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2];
+    const double Hn2 = r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2];
+    const double Hn[3] = {Hn0, Hn1, Hn2};
+    // T_ij += n_c H_ij - 1/2 (delta_ci (H n)_j + delta_cj (H n)_i)
+    const int kIdx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j) {
+        double d = r.h[kIdx[i][j]] * n[c];
+        if (i == c) d -= 0.5 * Hn[j];
+        if (j == c) d -= 0.5 * Hn[i];
+        T[kIdx[i][j]] = (IT)(T[kIdx[i][j]] + d);
+      }
+    nlap = (IT)(nlap + (r.h[0] + r.h[3] + r.h[5]) * n[c]);
+  }
+  Tri<IT> p;
+  interp_std<IT, float>(F.phi, G, y[0], y[1], y[2], p);
+
+  const double dA = y[12], dAp = y[13], s1 = y[14], s2 = y[15], el1 = y[16], el2 = y[17];
+  const double phi1 = 1.0 + 2.0 * p.v;
+  for (int i = 0; i < 3; ++i) dy[i] = -n[i] * phi1 - bval[i];
+  // -P_perp v with P_perp = n n^T - I  ->  v - n (n.v)
+  const double v0 = 2.0 * p.g[0] + ngB[0], v1 = 2.0 * p.g[1] + ngB[1], v2 = 2.0 * p.g[2] + ngB[2];
+  const double nv = n[0] * v0 + n[1] * v1 + n[2] * v2;
+  dy[3] = v0 - n[0] * nv;
+  dy[4] = v1 - n[1] * nv;
+  dy[5] = v2 - n[2] * nv;
+  const double ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
+  const double bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
+  for (int i = 0; i < 3; ++i) {
+    dy[6 + i] = -2.0 * n[i] * ag - n[i] * e1ngB;
+    dy[9 + i] = -2.0 * n[i] * bg - n[i] * e2ngB;
+  }
+  const double L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
+                   0.25 * (n[0] * ngB[0] + n[1] * ngB[1] + n[2] * ngB[2]);
+  // P_perp : H = n^T H n - tr H
+  const double nHn = n[0] * n[0] * p.h[0] + n[1] * n[1] * p.h[3] + n[2] * n[2] * p.h[5] +
+                     2.0 * (n[0] * n[1] * p.h[1] + n[0] * n[2] * p.h[2] + n[1] * n[2] * p.h[4]);
+  const double PH = nHn - (p.h[0] + p.h[3] + p.h[5]);
+  dy[12] = -dAp;
+  dy[13] = -4.0 * dAp * L - PH * dA + 0.5 * nlap * dA;
+  // effective tidal matrix H + T/2 projected on the shear basis
+  IT He[6];
+  for (int i = 0; i < 6; ++i) He[i] = (IT)(p.h[i] + 0.5 * T[i]);
+  const double S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
+                    (a[2] * a[2] - b[2] * b[2]) * He[5] +
+                    2.0 * ((a[0] * a[1] - b[0] * b[1]) * He[1] + (a[0] * a[2] - b[0] * b[2]) * He[2] +
+                           (a[1] * a[2] - b[1] * b[2]) * He[4]);
+  const double S2 = 2.0 * (a[0] * b[0] * He[0] + a[1] * b[1] * He[3] + a[2] * b[2] * He[5]) +
+                    2.0 * ((a[0] * b[1] + a[1] * b[0]) * He[1] + (a[0] * b[2] + a[2] * b[0]) * He[2] +
+                           (a[1] * b[2] + a[2] * b[1]) * He[4]);
+  dy[14] = 4.0 * s1 * L + S1 * dA * dA;
+  dy[15] = 4.0 * s2 * L + S2 * dA * dA;
+  if (dA > 0.5) {
+    const double dA2 = dA * dA;
+    const double q = sqrt(4.0 + el1 * el1 + el2 * el2);
+    dy[13] += (s1 * s1 + s2 * s2) / (dA2 * dA);
+    dy[16] = -2.0 * s1 * q / dA2;
+    dy[17] = -2.0 * s2 * q / dA2;
+    dy[18] = -(s1 * el2 - s2 * el1) / (dA2 * (2.0 + q));
+  } else {
+    dy[16] = 0.0;
+    dy[17] = 0.0;
+    dy[18] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------ ray geometry
+
+struct RayDir {  // sin/cos of the pixel centre's colatitude and longitude
+  double st, ct, sp, cp;
+};
+
+SRT_HD RayDir ray_dir(double theta, double phi) {
+  RayDir d;
+  d.st = sin(theta);
+  d.ct = cos(theta);
+  d.sp = sin(phi);
+  d.cp = cos(phi);
+  return d;
+}
+
+// Deflection from the displacement X = x_final - x_observer: the change of
+// direction X/|X| - r_hat projected on e_theta and on (sin phi, -cos phi, 0)
+// (snapshot-raytracer.cu:566-582).
+SRT_HD void extract_deflection(const RayDir& d, double X0, double X1, double X2, float* d1,
+                               float* d2) {
+  const double nrm = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
+  const double D0 = X0 / nrm - d.st * d.cp;
+  const double D1 = X1 / nrm - d.st * d.sp;
+  const double D2 = X2 / nrm - d.ct;
+  *d1 = (float)(D0 * d.ct * d.cp + D1 * d.ct * d.sp - D2 * d.st);
+  *d2 = (float)(D0 * d.sp - D1 * d.cp);
+}
+
+// ----------------------------------------------------- ray driver, FP64/REF16
+
+template <int MODE>
+SRT_HD void trace_ray_std(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps,
+                          float out[6]) {
+  double y[19], acc[19], k[19], ys[19];
+  y[0] = (double)G.n[0] * 0.5;
+  y[1] = (double)G.n[1] * 0.5;
+  y[2] = (double)G.n[2] * 0.5;
+  y[3] = -d.st * d.cp;
+  y[4] = -d.st * d.sp;
+  y[5] = -d.ct;
+  y[6] = d.ct * d.cp;
+  y[7] = d.ct * d.sp;
+  y[8] = -d.st;
+  y[9] = d.sp;
+  y[10] = -d.cp;
+  y[11] = 0.0;
+  y[12] = 0.0;
+  y[13] = -1.0;
+  for (int j = 14; j < 19; ++j) y[j] = 0.0;
+  for (int j = 0; j < 19; ++j) k[j] = 0.0;
+#pragma unroll 1
+  for (int step = 0; step < n_steps; ++step) {
+#pragma unroll 1
+    for (int st = 0; st < 4; ++st) {
+      const double c = (st == 3) ? 1.0 : 0.5;
+      for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
+      rhs_std<MODE>(ys, k, F, G);
+      for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.0 * k[j] : acc[j]);
+    }
+    for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) / 6.0;
+  }
+  out[0] = (float)y[12];
+  out[1] = (float)y[16];
+  out[2] = (float)y[17];
+  out[3] = (float)y[18];
+  extract_deflection(d, y[0] - (double)G.n[0] * 0.5, y[1] - (double)G.n[1] * 0.5,
+                     y[2] - (double)G.n[2] * 0.5, &out[4], &out[5]);
+}
+
+// -------------------------------------------------------------- MIXED mode
+
+// Exact two-term sum a + b = s + e.
+SRT_HD void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Cell and offset along one axis for the position th + lo (th, lo floats,
+// their sum exact); the cell is chosen from the exact sum.
+SRT_HD void locate(float th, float lo, int n, float invn, int& cell, float& t) {
+  const float fl = floorf(th);
+  float s, e;
+  two_sum(th - fl, lo, s, e);
+  float k = floorf(s);
+  if (s == k && e < 0.f) k -= 1.f;
+  t = (s - k) + e;
+  cell = wrap32((int)fl + (int)k, n, invn);
+}
+
+struct MixedRay {
+  float n0[3], a0[3], b0[3];  // FP32 bases of n, e1, e2
+  float eta[3];               // |base|^2 - 1 of the three bases
+  float x0[3];                // observer
+};
+
+// Unit vector of base + delta as (base + D): D = base (r - 1) + delta r with
+// r = (1 + q)^(-1/2), q = |base + delta|^2 - 1 = eta + 2 base.delta + delta^2.
+SRT_HD void unit_pert(const float* v0, const float* dv, float eta, float* D) {
+  const float q = eta + 2.f * (v0[0] * dv[0] + v0[1] * dv[1] + v0[2] * dv[2]) +
+                  (dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+  float rm1;
+  if (fabsf(q) < 1e-2f) {
+    rm1 = q * (-0.5f + q * (0.375f + q * (-0.3125f + q * 0.2734375f)));
+  } else {
+    const float s = sqrtf(1.f + q);
+    rm1 = -q / (s * (1.f + s));
+  }
+  for (int i = 0; i < 3; ++i) D[i] = v0[i] * rm1 + dv[i] * (1.f + rm1);
+}
+
+// Perturbation right-hand side g = f(y0(s) + d) - f(y0(s)) (FP32). `s` is the
+// affine parameter of the stage (step + 0, 1/2 or 1), d the stage state
+// (delta components in the layout of rhs_std).
+SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtrs& F,
+                      const Geom& G, float* g) {
+  float Dn[3], Da[3], Db[3];
+  unit_pert(R.n0, d + 3, R.eta[0], Dn);
+  unit_pert(R.a0, d + 6, R.eta[1], Da);
+  unit_pert(R.b0, d + 9, R.eta[2], Db);
+  float n[3], a[3], b[3];
+  for (int i = 0; i < 3; ++i) {
+    n[i] = R.n0[i] + Dn[i];
+    a[i] = R.a0[i] + Da[i];
+    b[i] = R.b0[i] + Db[i];
+  }
+  // ray position x0 - s n0 + d_x per axis as th + lo with th + lo exact
+  float th[3], lo[3];
+  for (int i = 0; i < 3; ++i) {
+    const float p = s * R.n0[i];
+    const float pe = fmaf(s, R.n0[i], -p);
+    float tl;
+    two_sum(R.x0[i], -p, th[i], tl);
+    lo[i] = (tl - pe) + d[i];
+  }
+  int cc[3], cs[3];
+  float tc[3], ts[3];
+  for (int i = 0; i < 3; ++i) {
+    locate(th[i], lo[i], G.n[i], G.invn[i], cc[i], tc[i]);          // centred
+    locate(th[i] - 0.5f, lo[i], G.n[i], G.invn[i], cs[i], ts[i]);   // staggered by -1/2
+  }
+  float bval[3], ngB[3] = {0.f, 0.f, 0.f}, e1ngB = 0.f, e2ngB = 0.f, nlap = 0.f;
+  float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    CRW<float> X, Y, Z;
+    cr_weights(c == 0 ? ts[0] : tc[0], X);
+    cr_weights(c == 1 ? ts[1] : tc[1], Y);
+    cr_weights(c == 2 ? ts[2] : tc[2], Z);
+    const int64_t base = cell_base(G, c == 0 ? cs[0] : cc[0], c == 1 ? cs[1] : cc[1],
+                                   c == 2 ? cs[2] : cc[2]);
+    Tri<float> r;
+    tricubic<float, float>(F.b[c], base, G.px, G.pxy, X, Y, Z, r);
+    bval[c] = r.v;
+    for (int i = 0; i < 3; ++i) ngB[i] += r.g[i] * n[c];
+    const float gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
+    const float ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
+    const float gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
+    e1ngB += 0.5f * (a[c] * gn + n[c] * ga);
+    e2ngB += 0.5f * (b[c] * gn + n[c] * gb);
+    const float Hn[3] = {r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2],
+                         r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2],
+                         r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2]};
+    const int kIdx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j) {
+        float dd = r.h[kIdx[i][j]] * n[c];
+        if (i == c) dd -= 0.5f * Hn[j];
+        if (j == c) dd -= 0.5f * Hn[i];
+        T[kIdx[i][j]] += dd;
+      }
+    nlap += (r.h[0] + r.h[3] + r.h[5]) * n[c];
+  }
+  Tri<float> p;
+  {
+    CRW<float> X, Y, Z;
+    cr_weights(tc[0], X);
+    cr_weights(tc[1], Y);
+    cr_weights(tc[2], Z);
+    tricubic<float, float>(F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy, X, Y, Z, p);
+  }
+  const float dA = s + d[12];
+  const float dAp = d[13] - 1.f;
+  const float s1 = d[14], s2 = d[15], el1 = d[16], el2 = d[17];
+  // x: f = -n (1 + 2 phi) - B, f0 = -n0
+  for (int i = 0; i < 3; ++i) g[i] = -Dn[i] - 2.f * p.v * n[i] - bval[i];
+  const float v0 = 2.f * p.g[0] + ngB[0], v1 = 2.f * p.g[1] + ngB[1], v2 = 2.f * p.g[2] + ngB[2];
+  const float nv = n[0] * v0 + n[1] * v1 + n[2] * v2;
+  g[3] = v0 - n[0] * nv;
+  g[4] = v1 - n[1] * nv;
+  g[5] = v2 - n[2] * nv;
+  const float ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
+  const float bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
+  for (int i = 0; i < 3; ++i) {
+    g[6 + i] = -n[i] * (2.f * ag + e1ngB);
+    g[9 + i] = -n[i] * (2.f * bg + e2ngB);
+  }
+  const float L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
+                  0.25f * (n[0] * ngB[0] + n[1] * ngB[1] + n[2] * ngB[2]);
+  const float nHn = n[0] * n[0] * p.h[0] + n[1] * n[1] * p.h[3] + n[2] * n[2] * p.h[5] +
+                    2.f * (n[0] * n[1] * p.h[1] + n[0] * n[2] * p.h[2] + n[1] * n[2] * p.h[4]);
+  const float PH = nHn - (p.h[0] + p.h[3] + p.h[5]);
+  g[12] = -d[13];  // f = -dA' = 1 - d13, f0 = 1
+  g[13] = -4.f * dAp * L - PH * dA + 0.5f * nlap * dA;
+  float He[6];
+  for (int i = 0; i < 6; ++i) He[i] = p.h[i] + 0.5f * T[i];
+  const float S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
+                   (a[2] * a[2] - b[2] * b[2]) * He[5] +
+                   2.f * ((a[0] * a[1] - b[0] * b[1]) * He[1] + (a[0] * a[2] - b[0] * b[2]) * He[2] +
+                          (a[1] * a[2] - b[1] * b[2]) * He[4]);
+  const float S2 = 2.f * (a[0] * b[0] * He[0] + a[1] * b[1] * He[3] + a[2] * b[2] * He[5]) +
+                   2.f * ((a[0] * b[1] + a[1] * b[0]) * He[1] + (a[0] * b[2] + a[2] * b[0]) * He[2] +
+                          (a[1] * b[2] + a[2] * b[1]) * He[4]);
+  const float dA2 = dA * dA;
+  g[14] = 4.f * s1 * L + S1 * dA2;
+  g[15] = 4.f * s2 * L + S2 * dA2;
+  // dA > 1/2  <=>  d12 > 1/2 - s (exact for the stage values of s)
+  if (d[12] > 0.5f - s) {
+    const float q = sqrtf(4.f + el1 * el1 + el2 * el2);
+    const float idA2 = 1.f / dA2;
+    g[13] += (s1 * s1 + s2 * s2) * idA2 / dA;
+    g[16] = -2.f * s1 * q * idA2;
+    g[17] = -2.f * s2 * q * idA2;
+    g[18] = -(s1 * el2 - s2 * el1) * idA2 / (2.f + q);
+  } else {
+    g[16] = 0.f;
+    g[17] = 0.f;
+    g[18] = 0.f;
+  }
+}
+
+SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps,
+                            float out[6]) {
+  MixedRay R;
+  float yh[19], yl[19], k[19], acc[19], ys[19];
+  {
+    const double n64[3] = {-d.st * d.cp, -d.st * d.sp, -d.ct};
+    const double a64[3] = {d.ct * d.cp, d.ct * d.sp, -d.st};
+    const double b64[3] = {d.sp, -d.cp, 0.0};
+    double qn = -1.0, qa = -1.0, qb = -1.0;
+    for (int i = 0; i < 3; ++i) {
+      R.n0[i] = (float)n64[i];
+      R.a0[i] = (float)a64[i];
+      R.b0[i] = (float)b64[i];
+      yh[3 + i] = (float)(n64[i] - (double)R.n0[i]);
+      yh[6 + i] = (float)(a64[i] - (double)R.a0[i]);
+      yh[9 + i] = (float)(b64[i] - (double)R.b0[i]);
+      qn += (double)R.n0[i] * (double)R.n0[i];
+      qa += (double)R.a0[i] * (double)R.a0[i];
+      qb += (double)R.b0[i] * (double)R.b0[i];
+      R.x0[i] = (float)((double)G.n[i] * 0.5);
+      yh[i] = 0.f;
+    }
+    R.eta[0] = (float)qn;
+    R.eta[1] = (float)qa;
+    R.eta[2] = (float)qb;
+  }
+  for (int j = 12; j < 19; ++j) yh[j] = 0.f;
+  for (int j = 0; j < 19; ++j) {
+    yl[j] = 0.f;
+    k[j] = 0.f;
+  }
+#pragma unroll 1
+  for (int step = 0; step < n_steps; ++step) {
+    const float s0 = (float)step;
+#pragma unroll 1
+    for (int st = 0; st < 4; ++st) {
+      const float c = (st == 3) ? 1.f : 0.5f;
+      for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? yh[j] + yl[j] : yh[j] + (yl[j] + c * k[j]);
+      rhs_mixed(ys, s0 + (st == 0 ? 0.f : c), R, F, G, k);
+      for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
+    }
+    for (int j = 0; j < 19; ++j) {
+      float sum, err;
+      two_sum(yh[j], (acc[j] + k[j]) * (1.f / 6.f), sum, err);
+      yh[j] = sum;
+      yl[j] += err;
+    }
+  }
+  const double S = (double)n_steps;
+  out[0] = (float)(S + (double)yh[12] + (double)yl[12]);
+  out[1] = yh[16] + yl[16];
+  out[2] = yh[17] + yl[17];
+  out[3] = yh[18] + yl[18];
+  double X[3];
+  for (int i = 0; i < 3; ++i) X[i] = -S * (double)R.n0[i] + ((double)yh[i] + (double)yl[i]);
+  extract_deflection(d, X[0], X[1], X[2], &out[4], &out[5]);
+}
+
+}  // namespace srt

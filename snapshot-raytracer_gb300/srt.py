@@ -1,0 +1,326 @@
+"""Python binding of libsrt (include/srt.h) over ctypes.
+
+This is the Python face of the drop-in boundary: it calls the C ABI with plain
+pointers (numpy arrays for host memory, torch CUDA tensors or raw integers for
+device memory) and raises SrtError with the library's message on any failure.
+The library must have been built (snapshot-raytracer_gb300/build_srt.py); there
+is no fallback implementation.
+
+Map order everywhere is MAP_NAMES, the reference's output order
+(snapshot-raytracer.cu:941-987).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libsrt.so")
+
+MAP_NAMES = ("dA", "ellipticity1", "ellipticity2", "rotation", "deflection1", "deflection2")
+PRECISION = {"fp64": 0, "mixed": 1, "ref16": 2}
+
+SRT_INPUT_DEVICE = 1
+SRT_OUTPUT_DEVICE = 2
+SRT_ASYNC = 4
+SRT_ACCUMULATE = 8
+SRT_DETERMINISTIC = 16
+
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
+          -5: "format error", -6: "no CUDA device", -7: "unsupported"}
+
+
+class SrtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "error"), code, msg))
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("trace_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("rays", ctypes.c_int64),
+                ("ray_steps", ctypes.c_int64), ("kernels", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
+                ("d2h_bytes", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_FP6 = ctypes.c_void_p * 6
+
+
+def lib():
+    """The loaded libsrt (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            raise RuntimeError("libsrt.so is not built (%s); run snapshot-raytracer_gb300/build_srt.py" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        sig = {
+            "srt_abi_version": (ctypes.c_int, []),
+            "srt_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+            "srt_device_count": (ctypes.c_int, []),
+            "srt_fields_create": (ctypes.c_int, [_P, _P, _I64, _I64, _I64, ctypes.c_uint, _P, ctypes.POINTER(_P)]),
+            "srt_fields_destroy": (ctypes.c_int, [_P]),
+            "srt_fields_bytes": (_I64, [_P]),
+            "srt_forward": (ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, ctypes.c_int, _FP6, ctypes.c_uint, _P,
+                                           ctypes.POINTER(Stats)]),
+            "srt_vjp": (ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, ctypes.c_int, _FP6, _P, _P, ctypes.c_int,
+                                       ctypes.c_uint, _P, ctypes.POINTER(Stats)]),
+            "srt_probe_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+            "srt_pix2ang_ring": (ctypes.c_int, [_I64, _I64, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_double)]),
+            "srt_nest2ring": (_I64, [_I64, _I64]),
+            "srt_ring2nest": (_I64, [_I64, _I64]),
+            "srt_h5_read_scalar": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_P),
+                                                  ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_int)]),
+            "srt_h5_read_vector3": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_P),
+                                                   ctypes.POINTER(_I64)]),
+            "srt_h5_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _P, ctypes.POINTER(_I64), ctypes.c_int,
+                                            ctypes.c_int]),
+            "srt_fits_write_map": (ctypes.c_int, [ctypes.c_char_p, _P, _I64, ctypes.c_int, ctypes.c_char_p,
+                                                  ctypes.c_int]),
+            "srt_fits_read_map": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P), ctypes.POINTER(_I64),
+                                                 ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_int)]),
+            "srt_free": (None, [_P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().srt_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc):
+    if rc != 0:
+        raise SrtError(rc, last_error())
+    return rc
+
+
+def device_count():
+    return lib().srt_device_count()
+
+
+def probe_peak(kind):
+    """Measured FMA rate of the current GPU in FLOP/s; kind 'fp32' or 'fp64'."""
+    v = ctypes.c_double()
+    _check(lib().srt_probe_peak({"fp32": 0, "fp64": 1}[kind], ctypes.byref(v)))
+    return v.value
+
+
+# --------------------------------------------------------------------- memory
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(x, want_device):
+    """(pointer, is_device) of a numpy array, torch tensor or raw int."""
+    if x is None:
+        return None, want_device
+    if isinstance(x, int):
+        return x, want_device
+    if _is_torch(x):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return x.data_ptr(), x.is_cuda
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return x.ctypes.data, False
+    raise TypeError("unsupported buffer type %r" % type(x))
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class Fields:
+    """Laid-out phi and B on the GPU (srt_fields_create). phi: (n2, n1, n0)
+    float32; b_xyz: (n2, n1, n0, 3) float32; numpy (host) or CUDA tensors."""
+
+    def __init__(self, phi, b_xyz, stream=None, async_=False):
+        shape = tuple(phi.shape)
+        if len(shape) != 3 or tuple(b_xyz.shape) != shape + (3,):
+            raise ValueError("phi must be (n2, n1, n0) and b_xyz (n2, n1, n0, 3); got %r and %r"
+                             % (shape, tuple(b_xyz.shape)))
+        for a in (phi, b_xyz):
+            if str(a.dtype).split(".")[-1] != "float32":
+                raise TypeError("fields must be float32")
+        p_phi, dev_phi = _ptr(phi, False)
+        p_b, dev_b = _ptr(b_xyz, False)
+        if dev_phi != dev_b:
+            raise ValueError("phi and b_xyz must both be on the host or both on the device")
+        self.n = (shape[2], shape[1], shape[0])
+        flags = (SRT_INPUT_DEVICE if dev_phi else 0) | (SRT_ASYNC if async_ else 0)
+        h = _P()
+        _check(lib().srt_fields_create(p_phi, p_b, self.n[0], self.n[1], self.n[2], flags, _stream_ptr(stream),
+                                       ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def nbytes(self):
+        return lib().srt_fields_bytes(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().srt_fields_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def forward(self, nside, n_steps, pix_begin=0, pix_count=None, precision="mixed", out=None, stream=None,
+                async_=False):
+        """Six maps of RING pixels [pix_begin, pix_begin + pix_count).
+        out: None (returns a new (6, count) float32 numpy array), a (6, count)
+        numpy array, or a (6, count) CUDA tensor (device output). Returns
+        (maps, Stats)."""
+        npix = 12 * nside * nside
+        if pix_count is None:
+            pix_count = npix - pix_begin
+        if out is None:
+            out = np.zeros((6, max(pix_count, 0)), np.float32)
+        p, dev = _ptr(out, False)
+        if tuple(out.shape) != (6, pix_count):
+            raise ValueError("out must have shape (6, %d)" % pix_count)
+        rows = _FP6(*[p + m * pix_count * 4 for m in range(6)])
+        st = Stats()
+        flags = (SRT_OUTPUT_DEVICE if dev else 0) | (SRT_ASYNC if async_ else 0)
+        _check(lib().srt_forward(self._h, nside, pix_begin, pix_count, n_steps, PRECISION[precision], rows, flags,
+                                 _stream_ptr(stream), ctypes.byref(st)))
+        return out, st
+
+    def vjp(self, nside, n_steps, weights, pix_begin=0, pix_count=None, precision="mixed", dphi=None, db_xyz=None,
+            ckpt_every=0, accumulate=False, deterministic=False, stream=None):
+        """Gradient of sum(weights * maps) w.r.t. phi and B (srt_vjp).
+        weights: (6, count) float32 (numpy or CUDA tensor). dphi / db_xyz:
+        outputs shaped like phi / b_xyz (numpy or CUDA tensors); new numpy
+        arrays when None. Returns (dphi, db_xyz, Stats)."""
+        npix = 12 * nside * nside
+        if pix_count is None:
+            pix_count = npix - pix_begin
+        n0, n1, n2 = self.n
+        if dphi is None:
+            dphi = np.zeros((n2, n1, n0), np.float32)
+        if db_xyz is None:
+            db_xyz = np.zeros((n2, n1, n0, 3), np.float32)
+        pw, wdev = _ptr(weights, False)
+        pg, gdev = _ptr(dphi, False)
+        pb, bdev = _ptr(db_xyz, False)
+        if not (wdev == gdev == bdev):
+            raise ValueError("weights and gradients must all be host or all be device buffers")
+        rows = _FP6(*[pw + m * pix_count * 4 for m in range(6)])
+        flags = (SRT_OUTPUT_DEVICE if wdev else 0) | (SRT_ACCUMULATE if accumulate else 0) | \
+            (SRT_DETERMINISTIC if deterministic else 0)
+        st = Stats()
+        _check(lib().srt_vjp(self._h, nside, pix_begin, pix_count, n_steps, PRECISION[precision], rows, pg, pb,
+                             ckpt_every, flags, _stream_ptr(stream), ctypes.byref(st)))
+        return dphi, db_xyz, st
+
+
+def trace(phi, b_xyz, nside, n_steps, batch=None, precision="mixed"):
+    """The CLI's computation (snapshot-raytracer.cu:708-717, :939-987): full
+    12*nside^2 RING maps, zero outside the batch's pixel range when batch is
+    given (batch b covers RING pixels [b*nside^2, (b+1)*nside^2))."""
+    npix = 12 * nside * nside
+    if batch is None:
+        begin, count = 0, npix
+    else:
+        if batch < 0 or batch * nside * nside >= npix:
+            raise ValueError("invalid batch %r" % batch)
+        begin, count = batch * nside * nside, nside * nside
+    with Fields(phi, b_xyz) as f:
+        part, _ = f.forward(nside, n_steps, begin, count, precision)
+    full = np.zeros((6, npix), np.float32)
+    full[:, begin:begin + count] = part
+    return full
+
+
+# -------------------------------------------------------------------- HEALPix
+
+def pix2ang_ring(nside, pix):
+    t, p = ctypes.c_double(), ctypes.c_double()
+    _check(lib().srt_pix2ang_ring(nside, pix, ctypes.byref(t), ctypes.byref(p)))
+    return t.value, p.value
+
+
+def nest2ring(nside, ipnest):
+    return lib().srt_nest2ring(nside, ipnest)
+
+
+def ring2nest(nside, ipring):
+    return lib().srt_ring2nest(nside, ipring)
+
+
+# ---------------------------------------------------------------------- files
+
+def _take_floats(ptr, count):
+    try:
+        arr = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_float)), shape=(count,)).copy()
+    finally:
+        lib().srt_free(ptr)
+    return arr
+
+
+def h5_read_scalar(path, dset="/data"):
+    """Float dataset of any rank as a numpy array shaped like the file's dims."""
+    p, dims, rank = _P(), (_I64 * 8)(), ctypes.c_int()
+    _check(lib().srt_h5_read_scalar(os.fsencode(path), dset.encode(), ctypes.byref(p), dims, ctypes.byref(rank)))
+    shape = tuple(dims[i] for i in range(rank.value))
+    return _take_floats(p, int(np.prod(shape))).reshape(shape)
+
+
+def h5_read_vector3(path, dset="/data"):
+    """Rank-3 dataset of array[3]-of-float elements as (d0, d1, d2, 3)."""
+    p, dims = _P(), (_I64 * 3)()
+    _check(lib().srt_h5_read_vector3(os.fsencode(path), dset.encode(), ctypes.byref(p), dims))
+    shape = (dims[0], dims[1], dims[2])
+    return _take_floats(p, 3 * int(np.prod(shape))).reshape(shape + (3,))
+
+
+def h5_write(path, data, dset="/data", vector3=False):
+    """Write float32 `data` as dataset `dset`; vector3 writes the last axis
+    (length 3) as an array[3] element type over the leading dims."""
+    a = np.ascontiguousarray(data, dtype=np.float32)
+    shape = a.shape[:-1] if vector3 else a.shape
+    if vector3 and a.shape[-1] != 3:
+        raise ValueError("vector3 data must end in an axis of length 3")
+    dims = (_I64 * len(shape))(*shape)
+    _check(lib().srt_h5_write(os.fsencode(path), dset.encode(), a.ctypes.data, dims, len(shape), int(vector3)))
+
+
+def fits_write_map(path, m, nside, nest=False, coordsys="C", overwrite=False):
+    a = np.ascontiguousarray(m, dtype=np.float32)
+    _check(lib().srt_fits_write_map(os.fsencode(path), a.ctypes.data, nside, int(nest), coordsys.encode(),
+                                    int(overwrite)))
+
+
+def fits_read_map(path):
+    """(map, nside, nest) of a HEALPix FITS map."""
+    p, npix, nside, nest = _P(), _I64(), _I64(), ctypes.c_int()
+    _check(lib().srt_fits_read_map(os.fsencode(path), ctypes.byref(p), ctypes.byref(npix), ctypes.byref(nside),
+                                   ctypes.byref(nest)))
+    return _take_floats(p, npix.value), nside.value, bool(nest.value)

@@ -1,0 +1,92 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "snapshot-raytracer_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+def _ensure_built():
+    import build_srt
+
+    if not (os.path.isfile(build_srt.LIBSRT) and os.path.isfile(build_srt.LIBORACLE)):
+        build_srt.build()
+
+
+_ensure_built()
+
+
+@pytest.fixture(scope="session")
+def srt():
+    import srt as _srt
+
+    return _srt
+
+
+@pytest.fixture(scope="session")
+def orc():
+    from oracle import oracle as _o
+
+    return _o
+
+
+@pytest.fixture(scope="session")
+def golden():
+    import json
+
+    import numpy as np
+
+    d = os.path.join(ROOT, "tests", "golden")
+    with open(os.path.join(d, "golden_cases.json")) as fh:
+        meta = json.load(fh)
+    maps = dict(np.load(os.path.join(d, "golden_maps.npz")))
+    return meta, maps
+
+
+def golden_fields(meta, case):
+    import numpy as np
+
+    import srt_fields
+
+    c = meta["cases"][case]
+    phi, b = srt_fields.int_noise_fields(tuple(c["extents"]), c["seed"])
+    if c["zero_fields"]:
+        phi, b = np.zeros_like(phi), np.zeros_like(b)
+    return phi, b
+
+
+def map_errors(a, b, ulps=1):
+    """Per map: (rms error, max error) relative to the rms of b's signal (for
+    dA, the rms of its fluctuation about the mean, since dA ~ n_steps).
+    Differences of up to `ulps` float32 spacings of b are the resolution of the
+    float32 maps themselves and are not counted."""
+    import numpy as np
+
+    out = []
+    for m in range(6):
+        d = a[m].astype(np.float64) - b[m].astype(np.float64)
+        d = np.sign(d) * np.maximum(np.abs(d) - ulps * np.spacing(np.abs(b[m])).astype(np.float64), 0.0)
+        r = b[m].astype(np.float64)
+        if m == 0:
+            r = r - r.mean()
+        s = np.sqrt(np.mean(r * r))
+        s = s if s > 0 else 1.0
+        out.append((np.sqrt(np.mean(d * d)) / s, np.abs(d).max() / s))
+    return out
+
+
+def has_gpu():
+    import srt
+
+    try:
+        return srt.device_count() > 0
+    except Exception:
+        return False

@@ -1,0 +1,177 @@
+"""GPU parity of the trace kernels (through the C ABI) against the oracle and
+against the golden vectors of the reference's own code.
+
+Tolerances (relative to the rms of each map's signal; for dA the rms of its
+fluctuation about the mean, see conftest.map_errors):
+  FP64  vs oracle FP64      rms <= 1e-9, max <= 1e-7   (only FMA contraction and
+                                                        libm ulps differ)
+  MIXED vs oracle FP64      rms <= 1e-5, max <= 1e-4   (the FP32 target)
+  REF16 vs reference golden rms <= 1e-5, max <= 2e-3   (same FP16/FP32 arithmetic,
+                                                        different FP32 rounding order)
+Pixel placement and batch masking are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+import srt_fields
+from conftest import golden_fields, map_errors
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["cube16_ns2_s12", "cube32_ns4_s24", "cube24_ns3_s20", "wrap16_ns2_s40", "batch5_cube32_ns4_s16",
+         "noncubic_16x20x24_ns2_s14"]
+TOL = {"fp64": (1e-9, 1e-7), "mixed": (1e-5, 1e-4), "ref16": (1e-5, 2e-3)}
+
+
+def _range(meta, case):
+    c = meta["cases"][case]
+    nside, batch = c["nside"], c["batch"]
+    if batch is None:
+        return nside, c["n_steps"], 0, 12 * nside * nside
+    return nside, c["n_steps"], batch * nside * nside, nside * nside
+
+
+def _assert_close(got, want, mode, what):
+    rms_t, max_t = TOL[mode]
+    errs = map_errors(got, want)
+    for m, (rms, mx) in enumerate(errs):
+        assert rms <= rms_t and mx <= max_t, "%s map %d: rms %.3g max %.3g (tol %.1g/%.1g)" % (
+            what, m, rms, mx, rms_t, max_t)
+    return errs
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_fp64_matches_oracle(golden, srt, orc, case):
+    meta, _ = golden
+    phi, b = golden_fields(meta, case)
+    nside, steps, begin, count = _range(meta, case)
+    with srt.Fields(phi, b) as f:
+        got, st = f.forward(nside, steps, begin, count, "fp64")
+    assert st.rays == count and st.ray_steps == count * steps and st.kernels >= 1
+    want = orc.trace(phi, b, nside, steps, begin, count, mode="fp64")
+    _assert_close(got, want, "fp64", case)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_mixed_matches_oracle(golden, srt, orc, case):
+    meta, _ = golden
+    phi, b = golden_fields(meta, case)
+    nside, steps, begin, count = _range(meta, case)
+    with srt.Fields(phi, b) as f:
+        got, _ = f.forward(nside, steps, begin, count, "mixed")
+    want = orc.trace(phi, b, nside, steps, begin, count, mode="fp64")
+    _assert_close(got, want, "mixed", case)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_ref16_matches_reference_golden(golden, srt, case):
+    meta, maps = golden
+    phi, b = golden_fields(meta, case)
+    nside, steps, begin, count = _range(meta, case)
+    with srt.Fields(phi, b) as f:
+        got, _ = f.forward(nside, steps, begin, count, "ref16")
+    _assert_close(got, maps[case][:, begin:begin + count], "ref16", case)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed", "ref16"])
+def test_zero_fields_exact(srt, mode):
+    n, nside, steps = 16, 4, 9
+    phi = np.zeros((n, n, n), np.float32)
+    b = np.zeros((n, n, n, 3), np.float32)
+    with srt.Fields(phi, b) as f:
+        m, _ = f.forward(nside, steps, precision=mode)
+    assert np.all(m[0] == steps)
+    assert not np.any(m[1:4])
+    assert np.abs(m[4:6]).max() < 1e-12
+
+
+def test_batches_tile_the_sky_bit_exact(srt):
+    """Batch b = RING pixels [b nside^2, (b+1) nside^2) (snapshot-raytracer.cu:708-717):
+    each batch's values equal the full-sky run's, bit for bit, and the CLI-style
+    full maps are zero outside the batch, so the 12 batches sum to the full sky."""
+    phi, b = srt_fields.int_noise_fields(32, seed=21)
+    nside, steps = 4, 10
+    for mode in ("mixed", "fp64"):
+        full = srt.trace(phi, b, nside, steps, precision=mode)
+        acc = np.zeros_like(full)
+        for batch in range(12):
+            part = srt.trace(phi, b, nside, steps, batch=batch, precision=mode)
+            lo, hi = batch * nside * nside, (batch + 1) * nside * nside
+            assert np.array_equal(part[:, lo:hi].view(np.uint32), full[:, lo:hi].view(np.uint32))
+            mask = np.ones(12 * nside * nside, bool)
+            mask[lo:hi] = False
+            assert not np.any(part[:, mask])
+            acc += part
+        assert np.array_equal(acc.view(np.uint32), full.view(np.uint32))
+    with pytest.raises(ValueError):
+        srt.trace(phi, b, nside, steps, batch=12)
+
+
+def test_arbitrary_ranges_and_empty(srt):
+    phi, b = srt_fields.int_noise_fields(16, seed=22)
+    with srt.Fields(phi, b) as f:
+        full, _ = f.forward(3, 7, precision="mixed")
+        part, _ = f.forward(3, 7, pix_begin=7, pix_count=13, precision="mixed")
+        assert np.array_equal(part.view(np.uint32), full[:, 7:20].view(np.uint32))
+        empty, st = f.forward(3, 7, pix_begin=5, pix_count=0)
+        assert empty.shape == (6, 0) and st.rays == 0
+        last, _ = f.forward(3, 7, pix_begin=107, pix_count=1, precision="mixed")
+        assert np.array_equal(last.view(np.uint32), full[:, 107:108].view(np.uint32))
+
+
+def test_invalid_arguments_raise(srt):
+    phi, b = srt_fields.int_noise_fields(16, seed=23)
+    with srt.Fields(phi, b) as f:
+        for kw in ({"nside": 0, "n_steps": 4}, {"nside": 2, "n_steps": 0}, {"nside": 2, "n_steps": 4, "pix_begin": 40},
+                   {"nside": 2, "n_steps": 4, "pix_begin": -1, "pix_count": 3}):
+            with pytest.raises((srt.SrtError, ValueError)):
+                f.forward(**kw)
+        with pytest.raises(KeyError):
+            f.forward(2, 4, precision="fp16")
+
+
+def test_deterministic(srt):
+    phi, b = srt_fields.gaussian_fields_np(32, seed=4)
+    with srt.Fields(phi, b) as f:
+        a, _ = f.forward(8, 20, precision="mixed")
+        c, _ = f.forward(8, 20, precision="mixed")
+    assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_gaussian_fields_vs_oracle(srt, orc, mode):
+    phi, b = srt_fields.gaussian_fields_np(64, seed=7)
+    nside, steps = 8, 48
+    with srt.Fields(phi, b) as f:
+        got, _ = f.forward(nside, steps, precision=mode)
+    want = orc.trace(phi, b, nside, steps, mode="fp64")
+    _assert_close(got, want, mode, "gaussian64")
+
+
+def test_device_buffers_match_host(srt):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    phi, b = srt_fields.gaussian_fields_np(32, seed=9)
+    with srt.Fields(phi, b) as f:
+        host, _ = f.forward(4, 16, precision="mixed")
+    tphi, tb = torch.from_numpy(phi).cuda(), torch.from_numpy(b).cuda()
+    out = torch.zeros((6, 192), dtype=torch.float32, device="cuda")
+    with srt.Fields(tphi, tb) as f:
+        f.forward(4, 16, precision="mixed", out=out)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), host.view(np.uint32))
+
+
+def test_larger_grid_mixed_vs_fp64_and_oracle_sample(srt, orc):
+    """256^3 / nside 64 / 128 steps (49k rays): MIXED against the all-FP64 GPU
+    form on every pixel, and the FP64 form against the oracle on a sample."""
+    phi, b = srt_fields.gaussian_fields_np(256, seed=12)
+    nside, steps = 64, 128
+    with srt.Fields(phi, b) as f:
+        m64, _ = f.forward(nside, steps, precision="fp64")
+        mmx, _ = f.forward(nside, steps, precision="mixed")
+    _assert_close(mmx, m64, "mixed", "mixed vs fp64 @256^3")
+    pix = np.random.default_rng(0).choice(12 * nside * nside, 96, replace=False)
+    want = orc.trace_pixels(phi, b, nside, steps, pix, mode="fp64")
+    _assert_close(m64[:, pix], want, "fp64", "fp64 sample @256^3")
