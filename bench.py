@@ -169,15 +169,9 @@ def max_over_ranks(x, world):
 
 
 def map_errors(a, b):
-    out = {}
-    for m, name in enumerate(MAP_NAMES):
-        d = a[m].astype(np.float64) - b[m].astype(np.float64)
-        r = b[m].astype(np.float64)
-        if m == 0:
-            r = r - r.mean()
-        s = max(float(np.sqrt(np.mean(r * r))), 1e-300)
-        out[name] = {"rms_rel": float(np.sqrt(np.mean(d * d)) / s), "max_rel": float(np.abs(d).max() / s)}
-    return out
+    from oracle.oracle import map_errors as _me
+
+    return {name: {"rms_rel": e[0], "max_rel": e[1]} for name, e in zip(MAP_NAMES, _me(a, b))}
 
 
 def sample_pixels(nside, count, begin=0, total=None, seed=0):

@@ -140,3 +140,23 @@ def ref_interp(phi, b, field, x, y, z):
     out = np.zeros(10, np.float64)
     ref_lib().srtref_interp(phi.ctypes.data, b.ctypes.data, n0, n1, n2, field, x, y, z, out.ctypes.data)
     return out
+
+
+def map_errors(a, b, ulps=1):
+    """Per map m: (rms error, max error) of maps `a` against the checker `b`,
+    relative to the rms of b's signal — for dA (map 0), the rms of its
+    fluctuation about the mean, since dA ~ n_steps. Differences of up to
+    `ulps` float32 spacings of b are the resolution of float32 maps and are
+    not counted."""
+    out = []
+    for m in range(6):
+        bm = np.asarray(b[m], np.float32)
+        d = np.asarray(a[m], np.float64) - bm.astype(np.float64)
+        d = np.sign(d) * np.maximum(np.abs(d) - ulps * np.spacing(np.abs(bm)).astype(np.float64), 0.0)
+        r = bm.astype(np.float64)
+        if m == 0:
+            r = r - r.mean()
+        s = float(np.sqrt(np.mean(r * r))) if r.size else 0.0
+        s = s if s > 0 else 1.0
+        out.append((float(np.sqrt(np.mean(d * d))) / s if d.size else 0.0, float(np.abs(d).max()) / s if d.size else 0.0))
+    return out

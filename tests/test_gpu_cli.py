@@ -1,0 +1,75 @@
+"""The CLI drop-in end to end on the GPU: HDF5 inputs -> six FITS maps with the
+reference's names, RING order, batch masking and stdout progress lines
+(snapshot-raytracer.cu:600-1007)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import srt_fields
+from conftest import PKG, golden_fields, map_errors
+
+pytestmark = pytest.mark.gpu
+CLI = os.path.join(PKG, "snapshot-raytracer")
+NAMES = ["dAmap", "ellipticity1map", "ellipticity2map", "rotationmap", "deflection1map", "deflection2map"]
+STDOUT = ["Nside: {nside}", "n_steps: {steps}", "Loading potential data from HDF5 file {phi} ...",
+          "Data dimensions: {d0} x {d1} x {d2}", "Loading B field data from HDF5 file {b} ...",
+          "Allocating device memory and copying data to device...", "Computing theta and phi angles...",
+          "Launching raytracing kernel...", "Raytracing completed.", "Saving results to FITS files...", "All done!"]
+
+
+def write_inputs(srt, tmp_path, phi, b):
+    pp, pb = str(tmp_path / "phi.h5"), str(tmp_path / "B.h5")
+    # HDF5 dims in file order; the reference takes dims[0] as the fastest extent
+    srt.h5_write(pp, phi)
+    srt.h5_write(pb, b, vector3=True)
+    return pp, pb
+
+
+@pytest.mark.parametrize("batch", [None, 3])
+def test_cli_maps_match_library(srt, tmp_path, batch):
+    phi, b = srt_fields.gaussian_fields_np(32, seed=5)
+    pp, pb = write_inputs(srt, tmp_path, phi, b)
+    nside, steps = 4, 16
+    args = [CLI, pp, pb, str(nside), str(steps)] + ([] if batch is None else [str(batch)])
+    r = subprocess.run(args, capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    want_out = [s.format(nside=nside, steps=steps, phi=pp, b=pb, d0=32, d1=32, d2=32) for s in STDOUT]
+    assert r.stdout.splitlines() == want_out
+    ref = srt.trace(phi, b, nside, steps, batch=batch, precision="mixed")
+    for m, name in enumerate(NAMES):
+        got, ns, nest = srt.fits_read_map(str(tmp_path / ("%s_batch%d.fits" % (name, 0 if batch is None else batch))))
+        assert ns == nside and not nest
+        assert np.array_equal(got.view(np.uint32), ref[m].view(np.uint32)), name
+
+
+def test_cli_ref16_reproduces_reference_golden(srt, golden, tmp_path):
+    meta, maps = golden
+    case = "batch5_cube32_ns4_s16"
+    phi, b = golden_fields(meta, case)
+    pp, pb = write_inputs(srt, tmp_path, phi, b)
+    c = meta["cases"][case]
+    r = subprocess.run([CLI, pp, pb, str(c["nside"]), str(c["n_steps"]), str(c["batch"]), "--precision", "ref16"],
+                       capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    got = np.stack([srt.fits_read_map(str(tmp_path / ("%s_batch%d.fits" % (n, c["batch"]))))[0] for n in NAMES])
+    want = maps[case]
+    outside = np.ones(want.shape[1], bool)
+    lo = c["batch"] * c["nside"] ** 2
+    outside[lo:lo + c["nside"] ** 2] = False
+    assert not np.any(got[:, outside])
+    for rms, mx in map_errors(got[:, ~outside], want[:, ~outside]):
+        assert rms < 1e-5 and mx < 2e-3
+
+
+def test_cli_keeps_existing_outputs(srt, tmp_path):
+    phi, b = srt_fields.int_noise_fields(16, seed=8)
+    pp, pb = write_inputs(srt, tmp_path, phi, b)
+    (tmp_path / "dAmap_batch0.fits").write_bytes(b"keep")
+    r = subprocess.run([CLI, pp, pb, "2", "4"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0 and "already exists" in r.stderr
+    assert (tmp_path / "dAmap_batch0.fits").read_bytes() == b"keep"
+    r = subprocess.run([CLI, pp, pb, "2", "4", "--overwrite"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0
+    assert srt.fits_read_map(str(tmp_path / "dAmap_batch0.fits"))[1] == 2

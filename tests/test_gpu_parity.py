@@ -122,7 +122,7 @@ def test_arbitrary_ranges_and_empty(srt):
 def test_invalid_arguments_raise(srt):
     phi, b = srt_fields.int_noise_fields(16, seed=23)
     with srt.Fields(phi, b) as f:
-        for kw in ({"nside": 0, "n_steps": 4}, {"nside": 2, "n_steps": 0}, {"nside": 2, "n_steps": 4, "pix_begin": 40},
+        for kw in ({"nside": 0, "n_steps": 4}, {"nside": 2, "n_steps": 0}, {"nside": 2, "n_steps": 4, "pix_begin": 49},
                    {"nside": 2, "n_steps": 4, "pix_begin": -1, "pix_count": 3}):
             with pytest.raises((srt.SrtError, ValueError)):
                 f.forward(**kw)
