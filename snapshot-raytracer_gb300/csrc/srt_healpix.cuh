@@ -37,9 +37,9 @@ SRT_HD int64_t hp_isqrt(int64_t v) {
   return r;
 }
 
-// Centre of RING pixel `pix`: z = cos(theta), st = sin(theta), phi.
-SRT_HD void hp_ring_zphi(int64_t nside, int64_t pix, double* z, double* st, double* phi) {
-  const double kPi = 3.141592653589793238462643383279502884;
+// Centre of RING pixel `pix`: z = cos(theta), st = sin(theta), and the
+// longitude as a fraction of pi, u = phi / pi.
+SRT_HD void hp_ring_zu(int64_t nside, int64_t pix, double* z, double* st, double* u) {
   const int64_t npix = 12 * nside * nside;
   const int64_t ncap = 2 * nside * (nside - 1);
   const double inv3n2 = 1.0 / (3.0 * (double)nside * (double)nside);
@@ -49,7 +49,7 @@ SRT_HD void hp_ring_zphi(int64_t nside, int64_t pix, double* z, double* st, doub
     const double t = (double)(i * i) * inv3n2;  // 1 - z
     *z = 1.0 - t;
     *st = sqrt(t * (2.0 - t));
-    *phi = (kPi / (2.0 * (double)i)) * ((double)j - 0.5);
+    *u = ((double)j - 0.5) / (2.0 * (double)i);
   } else if (pix < npix - ncap) {  // equatorial belt
     const int64_t q = pix - ncap;
     const int64_t i = q / (4 * nside) + nside;
@@ -58,7 +58,7 @@ SRT_HD void hp_ring_zphi(int64_t nside, int64_t pix, double* z, double* st, doub
     const double zz = (double)(2 * nside - i) * (2.0 / (3.0 * (double)nside));
     *z = zz;
     *st = sqrt((1.0 - zz) * (1.0 + zz));
-    *phi = (kPi / (2.0 * (double)nside)) * ((double)j - f);
+    *u = ((double)j - f) / (2.0 * (double)nside);
   } else {  // south polar cap
     const int64_t q = npix - pix;
     const int64_t i = (1 + hp_isqrt(2 * q - 1)) >> 1;
@@ -66,8 +66,15 @@ SRT_HD void hp_ring_zphi(int64_t nside, int64_t pix, double* z, double* st, doub
     const double t = (double)(i * i) * inv3n2;  // 1 + z
     *z = t - 1.0;
     *st = sqrt(t * (2.0 - t));
-    *phi = (kPi / (2.0 * (double)i)) * ((double)j - 0.5);
+    *u = ((double)j - 0.5) / (2.0 * (double)i);
   }
+}
+
+// Same centre with the longitude in radians.
+SRT_HD void hp_ring_zphi(int64_t nside, int64_t pix, double* z, double* st, double* phi) {
+  double u;
+  hp_ring_zu(nside, pix, z, st, &u);
+  *phi = 3.141592653589793238462643383279502884 * u;
 }
 
 // theta, phi of a RING pixel centre (theta from atan2 of the exact sin/cos pair).

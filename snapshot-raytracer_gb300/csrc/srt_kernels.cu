@@ -67,8 +67,14 @@ cudaError_t launch_quantize_half(const float* src, __half* dst, int64_t count, c
 
 // -------------------------------------------------------------------- trace
 
+// Resident blocks of 128 threads per SM the mixed kernel is compiled for
+// (register budget 65536 / (128 * blocks)).
+#ifndef SRT_MIXED_MIN_BLOCKS
+#define SRT_MIXED_MIN_BLOCKS 2
+#endif
+
 template <int MODE>
-__global__ void __launch_bounds__(128) trace_kernel(const TraceArgs A) {
+__global__ void __launch_bounds__(128, MODE == kMIXED ? SRT_MIXED_MIN_BLOCKS : 1) trace_kernel(const TraceArgs A) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.launch_rays) return;
   // launch order: face-major, Morton (NESTED for power-of-two nside) in-face
@@ -79,9 +85,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const TraceArgs A) {
   const int64_t ring = hp_xyf2ring(A.nside, ix, iy, (int)face);
   const int64_t o = ring - A.pix_begin;
   if (o < 0 || o >= A.pix_count) return;
-  double z, st, ph;
-  hp_ring_zphi(A.nside, ring, &z, &st, &ph);
-  const RayDir d = ray_dir(atan2(st, z), ph);
+  const RayDir d = ray_dir_pix(A.nside, ring);
   float out[6];
   if (MODE == kMIXED)
     trace_ray_mixed(A.F, A.G, d, A.n_steps, out);

@@ -407,31 +407,69 @@ SRT_HD void locate(float th, float lo, int n, float invn, int& cell, float& t) {
 }
 
 struct MixedRay {
-  float n0[3], a0[3], b0[3];  // FP32 bases of n, e1, e2
+  float n0[3], a0[3], b0[3];  // FP32 bases of n, e1, e2 (straight-ray solution)
   float eta[3];               // |base|^2 - 1 of the three bases
-  float x0[3];                // observer
+  float dn0[3];               // FP64 direction minus its FP32 base (for the extraction)
 };
+
+// (1 + q)^(-1/2) - 1 for |q| << 1 without cancellation.
+SRT_HD float rsqrt1p_m1(float q) {
+  if (fabsf(q) < 1e-2f) return q * (-0.5f + q * (0.375f + q * (-0.3125f + q * 0.2734375f)));
+  const float s = sqrtf(1.f + q);
+  return -q / (s * (1.f + s));
+}
 
 // Unit vector of base + delta as (base + D): D = base (r - 1) + delta r with
 // r = (1 + q)^(-1/2), q = |base + delta|^2 - 1 = eta + 2 base.delta + delta^2.
 SRT_HD void unit_pert(const float* v0, const float* dv, float eta, float* D) {
   const float q = eta + 2.f * (v0[0] * dv[0] + v0[1] * dv[1] + v0[2] * dv[2]) +
                   (dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-  float rm1;
-  if (fabsf(q) < 1e-2f) {
-    rm1 = q * (-0.5f + q * (0.375f + q * (-0.3125f + q * 0.2734375f)));
-  } else {
-    const float s = sqrtf(1.f + q);
-    rm1 = -q / (s * (1.f + s));
-  }
+  const float rm1 = rsqrt1p_m1(q);
   for (int i = 0; i < 3; ++i) D[i] = v0[i] * rm1 + dv[i] * (1.f + rm1);
+}
+
+// Quantities the B components contribute to the right-hand side
+// (snapshot-raytracer.cu:377-460), accumulated component by component.
+struct BAcc {
+  float val[3], ngB[3], e1ngB, e2ngB, nlap, T[6];
+};
+
+// B component C interpolated at the position staggered by -1/2 along axis C,
+// folded into the accumulators. C is a compile-time constant so n[C], a[C]
+// and b[C] stay in registers.
+template <int C>
+SRT_HD void add_b_component(const float* __restrict__ field, const Geom& G, const int* cc, const int* cs,
+                            const float* ts, const CRW<float>& Cx, const CRW<float>& Cy, const CRW<float>& Cz,
+                            const float* n, const float* a, const float* b, BAcc& A) {
+  CRW<float> S;
+  cr_weights(ts[C], S);
+  const int64_t base = cell_base(G, C == 0 ? cs[0] : cc[0], C == 1 ? cs[1] : cc[1], C == 2 ? cs[2] : cc[2]);
+  Tri<float> r;
+  tricubic<float, float>(field, base, G.px, G.pxy, C == 0 ? S : Cx, C == 1 ? S : Cy, C == 2 ? S : Cz, r);
+  A.val[C] = r.v;
+  for (int i = 0; i < 3; ++i) A.ngB[i] += r.g[i] * n[C];
+  const float gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
+  const float ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
+  const float gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
+  A.e1ngB += 0.5f * (a[C] * gn + n[C] * ga);
+  A.e2ngB += 0.5f * (b[C] * gn + n[C] * gb);
+  const float Hn[3] = {r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2], r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2],
+                       r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2]};
+  // T_ij += n_C H_ij - 1/2 (delta_Ci (H n)_j + delta_Cj (H n)_i), ij in xx xy xz yy yz zz
+  A.T[0] += r.h[0] * n[C] - (C == 0 ? Hn[0] : 0.f);
+  A.T[1] += r.h[1] * n[C] - 0.5f * (C == 0 ? Hn[1] : (C == 1 ? Hn[0] : 0.f));
+  A.T[2] += r.h[2] * n[C] - 0.5f * (C == 0 ? Hn[2] : (C == 2 ? Hn[0] : 0.f));
+  A.T[3] += r.h[3] * n[C] - (C == 1 ? Hn[1] : 0.f);
+  A.T[4] += r.h[4] * n[C] - 0.5f * (C == 1 ? Hn[2] : (C == 2 ? Hn[1] : 0.f));
+  A.T[5] += r.h[5] * n[C] - (C == 2 ? Hn[2] : 0.f);
+  A.nlap += (r.h[0] + r.h[3] + r.h[5]) * n[C];
 }
 
 // Perturbation right-hand side g = f(y0(s) + d) - f(y0(s)) (FP32). `s` is the
 // affine parameter of the stage (step + 0, 1/2 or 1), d the stage state
-// (delta components in the layout of rhs_std).
-SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtrs& F,
-                      const Geom& G, float* g) {
+// (delta components in the layout of rhs_std), x0 the observer.
+SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtrs& F, const Geom& G,
+                      const float* x0, float* g) {
   float Dn[3], Da[3], Db[3];
   unit_pert(R.n0, d + 3, R.eta[0], Dn);
   unit_pert(R.a0, d + 6, R.eta[1], Da);
@@ -443,66 +481,37 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
     b[i] = R.b0[i] + Db[i];
   }
   // ray position x0 - s n0 + d_x per axis as th + lo with th + lo exact
-  float th[3], lo[3];
-  for (int i = 0; i < 3; ++i) {
-    const float p = s * R.n0[i];
-    const float pe = fmaf(s, R.n0[i], -p);
-    float tl;
-    two_sum(R.x0[i], -p, th[i], tl);
-    lo[i] = (tl - pe) + d[i];
-  }
   int cc[3], cs[3];
   float tc[3], ts[3];
   for (int i = 0; i < 3; ++i) {
-    locate(th[i], lo[i], G.n[i], G.invn[i], cc[i], tc[i]);          // centred
-    locate(th[i] - 0.5f, lo[i], G.n[i], G.invn[i], cs[i], ts[i]);   // staggered by -1/2
+    const float p = s * R.n0[i];
+    const float pe = fmaf(s, R.n0[i], -p);
+    float th, tl;
+    two_sum(x0[i], -p, th, tl);
+    const float lo = (tl - pe) + d[i];
+    locate(th, lo, G.n[i], G.invn[i], cc[i], tc[i]);          // centred
+    locate(th - 0.5f, lo, G.n[i], G.invn[i], cs[i], ts[i]);   // staggered by -1/2
   }
-  float bval[3], ngB[3] = {0.f, 0.f, 0.f}, e1ngB = 0.f, e2ngB = 0.f, nlap = 0.f;
-  float T[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    CRW<float> X, Y, Z;
-    cr_weights(c == 0 ? ts[0] : tc[0], X);
-    cr_weights(c == 1 ? ts[1] : tc[1], Y);
-    cr_weights(c == 2 ? ts[2] : tc[2], Z);
-    const int64_t base = cell_base(G, c == 0 ? cs[0] : cc[0], c == 1 ? cs[1] : cc[1],
-                                   c == 2 ? cs[2] : cc[2]);
-    Tri<float> r;
-    tricubic<float, float>(F.b[c], base, G.px, G.pxy, X, Y, Z, r);
-    bval[c] = r.v;
-    for (int i = 0; i < 3; ++i) ngB[i] += r.g[i] * n[c];
-    const float gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
-    const float ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
-    const float gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
-    e1ngB += 0.5f * (a[c] * gn + n[c] * ga);
-    e2ngB += 0.5f * (b[c] * gn + n[c] * gb);
-    const float Hn[3] = {r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2],
-                         r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2],
-                         r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2]};
-    const int kIdx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-    for (int i = 0; i < 3; ++i)
-      for (int j = i; j < 3; ++j) {
-        float dd = r.h[kIdx[i][j]] * n[c];
-        if (i == c) dd -= 0.5f * Hn[j];
-        if (j == c) dd -= 0.5f * Hn[i];
-        T[kIdx[i][j]] += dd;
-      }
-    nlap += (r.h[0] + r.h[3] + r.h[5]) * n[c];
-  }
+  CRW<float> Cx, Cy, Cz;  // centred weights, shared by phi and two axes of each B component
+  cr_weights(tc[0], Cx);
+  cr_weights(tc[1], Cy);
+  cr_weights(tc[2], Cz);
+  BAcc A;
+  A.ngB[0] = A.ngB[1] = A.ngB[2] = 0.f;
+  A.e1ngB = A.e2ngB = A.nlap = 0.f;
+  for (int i = 0; i < 6; ++i) A.T[i] = 0.f;
+  add_b_component<0>(F.b[0], G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
+  add_b_component<1>(F.b[1], G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
+  add_b_component<2>(F.b[2], G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
   Tri<float> p;
-  {
-    CRW<float> X, Y, Z;
-    cr_weights(tc[0], X);
-    cr_weights(tc[1], Y);
-    cr_weights(tc[2], Z);
-    tricubic<float, float>(F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy, X, Y, Z, p);
-  }
+  tricubic<float, float>(F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy, Cx, Cy, Cz, p);
+
   const float dA = s + d[12];
   const float dAp = d[13] - 1.f;
   const float s1 = d[14], s2 = d[15], el1 = d[16], el2 = d[17];
   // x: f = -n (1 + 2 phi) - B, f0 = -n0
-  for (int i = 0; i < 3; ++i) g[i] = -Dn[i] - 2.f * p.v * n[i] - bval[i];
-  const float v0 = 2.f * p.g[0] + ngB[0], v1 = 2.f * p.g[1] + ngB[1], v2 = 2.f * p.g[2] + ngB[2];
+  for (int i = 0; i < 3; ++i) g[i] = -Dn[i] - 2.f * p.v * n[i] - A.val[i];
+  const float v0 = 2.f * p.g[0] + A.ngB[0], v1 = 2.f * p.g[1] + A.ngB[1], v2 = 2.f * p.g[2] + A.ngB[2];
   const float nv = n[0] * v0 + n[1] * v1 + n[2] * v2;
   g[3] = v0 - n[0] * nv;
   g[4] = v1 - n[1] * nv;
@@ -510,18 +519,18 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   const float ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
   const float bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
   for (int i = 0; i < 3; ++i) {
-    g[6 + i] = -n[i] * (2.f * ag + e1ngB);
-    g[9 + i] = -n[i] * (2.f * bg + e2ngB);
+    g[6 + i] = -n[i] * (2.f * ag + A.e1ngB);
+    g[9 + i] = -n[i] * (2.f * bg + A.e2ngB);
   }
   const float L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
-                  0.25f * (n[0] * ngB[0] + n[1] * ngB[1] + n[2] * ngB[2]);
+                  0.25f * (n[0] * A.ngB[0] + n[1] * A.ngB[1] + n[2] * A.ngB[2]);
   const float nHn = n[0] * n[0] * p.h[0] + n[1] * n[1] * p.h[3] + n[2] * n[2] * p.h[5] +
                     2.f * (n[0] * n[1] * p.h[1] + n[0] * n[2] * p.h[2] + n[1] * n[2] * p.h[4]);
   const float PH = nHn - (p.h[0] + p.h[3] + p.h[5]);
   g[12] = -d[13];  // f = -dA' = 1 - d13, f0 = 1
-  g[13] = -4.f * dAp * L - PH * dA + 0.5f * nlap * dA;
+  g[13] = -4.f * dAp * L - PH * dA + 0.5f * A.nlap * dA;
   float He[6];
-  for (int i = 0; i < 6; ++i) He[i] = p.h[i] + 0.5f * T[i];
+  for (int i = 0; i < 6; ++i) He[i] = p.h[i] + 0.5f * A.T[i];
   const float S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
                    (a[2] * a[2] - b[2] * b[2]) * He[5] +
                    2.f * ((a[0] * a[1] - b[0] * b[1]) * He[1] + (a[0] * a[2] - b[0] * b[2]) * He[2] +
@@ -547,10 +556,15 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   }
 }
 
-SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps,
-                            float out[6]) {
+// Number of leading state components accumulated with a compensation term:
+// the ray position, whose increments are ~1e-4 of its size after a few hundred
+// steps and whose error becomes the deflection error.
+constexpr int kCompensated = 3;
+
+SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6]) {
   MixedRay R;
-  float yh[19], yl[19], k[19], acc[19], ys[19];
+  float yh[19], yl[kCompensated], k[19], acc[19], ys[19];
+  const float x0[3] = {(float)((double)G.n[0] * 0.5), (float)((double)G.n[1] * 0.5), (float)((double)G.n[2] * 0.5)};
   {
     const double n64[3] = {-d.st * d.cp, -d.st * d.sp, -d.ct};
     const double a64[3] = {d.ct * d.cp, d.ct * d.sp, -d.st};
@@ -560,13 +574,13 @@ SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, 
       R.n0[i] = (float)n64[i];
       R.a0[i] = (float)a64[i];
       R.b0[i] = (float)b64[i];
-      yh[3 + i] = (float)(n64[i] - (double)R.n0[i]);
+      R.dn0[i] = (float)(n64[i] - (double)R.n0[i]);
+      yh[3 + i] = R.dn0[i];
       yh[6 + i] = (float)(a64[i] - (double)R.a0[i]);
       yh[9 + i] = (float)(b64[i] - (double)R.b0[i]);
       qn += (double)R.n0[i] * (double)R.n0[i];
       qa += (double)R.a0[i] * (double)R.a0[i];
       qb += (double)R.b0[i] * (double)R.b0[i];
-      R.x0[i] = (float)((double)G.n[i] * 0.5);
       yh[i] = 0.f;
     }
     R.eta[0] = (float)qn;
@@ -574,35 +588,63 @@ SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, 
     R.eta[2] = (float)qb;
   }
   for (int j = 12; j < 19; ++j) yh[j] = 0.f;
-  for (int j = 0; j < 19; ++j) {
-    yl[j] = 0.f;
-    k[j] = 0.f;
-  }
+  for (int j = 0; j < kCompensated; ++j) yl[j] = 0.f;
+  for (int j = 0; j < 19; ++j) k[j] = 0.f;
 #pragma unroll 1
   for (int step = 0; step < n_steps; ++step) {
     const float s0 = (float)step;
 #pragma unroll 1
     for (int st = 0; st < 4; ++st) {
-      const float c = (st == 3) ? 1.f : 0.5f;
-      for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? yh[j] + yl[j] : yh[j] + (yl[j] + c * k[j]);
-      rhs_mixed(ys, s0 + (st == 0 ? 0.f : c), R, F, G, k);
+      const float c = (st == 0) ? 0.f : ((st == 3) ? 1.f : 0.5f);
+      for (int j = 0; j < kCompensated; ++j) ys[j] = yh[j] + (yl[j] + c * k[j]);
+      for (int j = kCompensated; j < 19; ++j) ys[j] = yh[j] + c * k[j];
+      rhs_mixed(ys, s0 + c, R, F, G, x0, k);
       for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
     }
-    for (int j = 0; j < 19; ++j) {
+    for (int j = 0; j < kCompensated; ++j) {
       float sum, err;
       two_sum(yh[j], (acc[j] + k[j]) * (1.f / 6.f), sum, err);
       yh[j] = sum;
       yl[j] += err;
     }
+    for (int j = kCompensated; j < 19; ++j) yh[j] += (acc[j] + k[j]) * (1.f / 6.f);
   }
-  const double S = (double)n_steps;
-  out[0] = (float)(S + (double)yh[12] + (double)yl[12]);
-  out[1] = yh[16] + yl[16];
-  out[2] = yh[17] + yl[17];
-  out[3] = yh[18] + yl[18];
-  double X[3];
-  for (int i = 0; i < 3; ++i) X[i] = -S * (double)R.n0[i] + ((double)yh[i] + (double)yl[i]);
-  extract_deflection(d, X[0], X[1], X[2], &out[4], &out[5]);
+  // Extraction in FP32 on the perturbation: the displacement is
+  // X = -S n0 + dx = S (-n0 + u), u = dx / S; X/|X| - r_hat = dn0 + u (1 + c) - n0 c
+  // with c = |(-n0 + u)|^-1 - 1 and r_hat = -(n0 + dn0) (snapshot-raytracer.cu:566-582).
+  const float S = (float)n_steps;
+  float u[3];
+  for (int i = 0; i < 3; ++i) u[i] = (yh[i] + yl[i]) / S;
+  const float q = R.eta[0] - 2.f * (R.n0[0] * u[0] + R.n0[1] * u[1] + R.n0[2] * u[2]) +
+                  (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  const float cc = rsqrt1p_m1(q);
+  float D[3];
+  for (int i = 0; i < 3; ++i) D[i] = R.dn0[i] + u[i] * (1.f + cc) - R.n0[i] * cc;
+  out[4] = D[0] * R.a0[0] + D[1] * R.a0[1] + D[2] * R.a0[2];
+  out[5] = D[0] * R.b0[0] + D[1] * R.b0[1] + D[2] * R.b0[2];
+  float dsum, derr;
+  two_sum(S, yh[12], dsum, derr);
+  out[0] = dsum + derr;
+  out[1] = yh[16];
+  out[2] = yh[17];
+  out[3] = yh[18];
+}
+
+// Ray direction of a RING pixel centre (FP64: cos/sin of the colatitude from
+// the ring geometry, sin/cos of pi * u for the longitude).
+SRT_HD RayDir ray_dir_pix(int64_t nside, int64_t ring) {
+  double z, st, u;
+  hp_ring_zu(nside, ring, &z, &st, &u);
+  RayDir d;
+  d.st = st;
+  d.ct = z;
+#if defined(__CUDA_ARCH__)
+  sincospi(u, &d.sp, &d.cp);
+#else
+  d.sp = sin(3.141592653589793238462643383279502884 * u);
+  d.cp = cos(3.141592653589793238462643383279502884 * u);
+#endif
+  return d;
 }
 
 }  // namespace srt
