@@ -160,3 +160,44 @@ def map_errors(a, b, ulps=1):
         s = s if s > 0 else 1.0
         out.append((float(np.sqrt(np.mean(d * d))) / s if d.size else 0.0, float(np.abs(d).max()) / s if d.size else 0.0))
     return out
+
+
+def tangent(phi, b, nside, n_steps, pixels, weights, dir_phi=(), dir_b=(), threads=0):
+    """FP64 loss L = sum_m sum_i weights[m, i] map_m(pixels[i]) (maps before the
+    float cast) and its derivatives along grid directions (forward mode, up to
+    8 per call): dir_phi[k] shaped like phi, dir_b[k] like b (None = zero).
+    Returns (L, [dL_k])."""
+    L_ = lib()
+    if not hasattr(L_, "_tangent_sig"):
+        L_.srto_tangent.argtypes = [_P, _P, _I64, _I64, _I64, _I64, _P, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_int,
+                                    _P, _P, ctypes.c_int]
+        L_._tangent_sig = True
+    phi, b, n0, n1, n2 = _dims(phi, b)
+    pix = np.ascontiguousarray(pixels, np.int64)
+    w = np.ascontiguousarray(weights, np.float32).reshape(6, len(pix))
+    nd = max(len(dir_phi), len(dir_b))
+    if nd > 8:
+        raise ValueError("at most 8 directions per call")
+    keep = []
+
+    def arr(lst, shape):
+        ptrs = (ctypes.c_void_p * max(nd, 1))()
+        for k in range(nd):
+            a = lst[k] if k < len(lst) else None
+            if a is not None:
+                a = np.ascontiguousarray(a, np.float32)
+                assert a.shape == shape
+                keep.append(a)
+                ptrs[k] = a.ctypes.data
+        return ptrs
+
+    pp = arr(list(dir_phi), phi.shape)
+    pb = arr(list(dir_b), b.shape)
+    out = ctypes.c_double()
+    dl = np.zeros(max(nd, 1), np.float64)
+    rc = L_.srto_tangent(phi.ctypes.data, b.ctypes.data, n0, n1, n2, nside, pix.ctypes.data, len(pix), n_steps,
+                         w.ctypes.data, ctypes.cast(pp, _P), ctypes.cast(pb, _P), nd, ctypes.byref(out),
+                         dl.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError("srto_tangent failed (%d)" % rc)
+    return out.value, list(dl[:nd])

@@ -61,9 +61,16 @@ def _gxx_obj(src, verbose):
 
 
 def build_oracle(verbose=False):
-    """The CPU oracle (test infrastructure)."""
-    _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-          "-o", LIBORACLE, os.path.join(ORACLE_DIR, "srt_oracle.c"), "-lm"], verbose)
+    """The CPU oracle (test infrastructure): the C restatement and its
+    dual-number tangent, no FMA contraction."""
+    os.makedirs(BUILD, exist_ok=True)
+    o1 = os.path.join(BUILD, "srt_oracle.o")
+    o2 = os.path.join(BUILD, "srt_oracle_tangent.o")
+    _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-c",
+          os.path.join(ORACLE_DIR, "srt_oracle.c"), "-o", o1], verbose)
+    _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-c",
+          os.path.join(ORACLE_DIR, "srt_oracle_tangent.cpp"), "-o", o2], verbose)
+    _run(["g++", "-shared", "-fopenmp", "-o", LIBORACLE, o1, o2, "-lm"], verbose)
     return LIBORACLE
 
 

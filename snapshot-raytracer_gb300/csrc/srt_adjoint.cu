@@ -1,2 +1,594 @@
-// srt_adjoint.cu — reverse-mode (vjp) kernels of the tracer (placeholder).
+// srt_adjoint.cu — vjp of the six maps with respect to the phi and B grids
+// (srt_vjp in include/srt.h). The reference has no derivatives; what is
+// differentiated is its forward scheme, snapshot-raytracer.cu:315-583, as
+// restated in srt_scheme.cuh.
+//
+// Kernels (one thread per ray, rays in the forward's launch order):
+//   ray_count_kernel / ray_write_kernel  Morton-ordered list of the RING pixels
+//                                        of the requested range
+//   ckpt_kernel<MODE>      forward trace storing the state every C steps
+//                          (and the final state) in device memory
+//   reverse_kernel<MODE>   per segment, backwards: recompute the segment from
+//                          its checkpoint storing y_i, k1, k2, k3 per step;
+//                          then per step, backwards, the RK4 adjoint
+//                            a4 = J(u4)^T l/6, a3 = J(u3)^T (l/3 + a4),
+//                            a2 = J(u2)^T (l/3 + a3/2), a1 = J(u1)^T (l/6 + a2/2),
+//                            l <- l + a1 + a2 + a3 + a4,
+//                          scattering the tap cotangents into halo-padded
+//                          gradient grids (FP32 atomics, FP64 atomics, or
+//                          64-bit fixed point for SRT_DETERMINISTIC)
+//   fold_kernel            sums the halo copies of each voxel back onto the
+//                          periodic grid and writes the caller's layout
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
+#include "srt_adjoint.cuh"
 #include "srt_internal.h"
+
+namespace srt {
+
+// ------------------------------------------------------------- ray list
+
+struct RangeArgs {
+  int64_t nside, pix_begin, pix_count, launch_rays;
+  int log2p;
+};
+
+__device__ __forceinline__ int64_t ring_of_slot(const RangeArgs& a, int64_t t) {
+  if (t >= a.launch_rays) return -1;
+  const int64_t face = t >> (2 * a.log2p);
+  int64_t ix, iy;
+  hp_deinterleave(t & ((int64_t(1) << (2 * a.log2p)) - 1), &ix, &iy);
+  if (ix >= a.nside || iy >= a.nside) return -1;
+  const int64_t ring = hp_xyf2ring(a.nside, ix, iy, (int)face);
+  return (ring >= a.pix_begin && ring < a.pix_begin + a.pix_count) ? ring : -1;
+}
+
+constexpr int kListBlock = 256;
+
+__global__ void ray_count_kernel(const RangeArgs a, int* counts) {
+  const int64_t t = (int64_t)blockIdx.x * kListBlock + threadIdx.x;
+  const int in = ring_of_slot(a, t) >= 0;
+  const int c = __syncthreads_count(in);
+  if (threadIdx.x == 0) counts[blockIdx.x] = c;
+}
+
+__global__ void ray_write_kernel(const RangeArgs a, const int64_t* offsets, int64_t* rays) {
+  __shared__ int warp_tot[kListBlock / 32];
+  const int64_t t = (int64_t)blockIdx.x * kListBlock + threadIdx.x;
+  const int64_t ring = ring_of_slot(a, t);
+  const unsigned mask = __ballot_sync(0xffffffffu, ring >= 0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warp_tot[warp] = __popc(mask);
+  __syncthreads();
+  int before = 0;
+  for (int w = 0; w < warp; ++w) before += warp_tot[w];
+  if (ring >= 0) rays[offsets[blockIdx.x] + before + __popc(mask & ((1u << lane) - 1u))] = ring;
+}
+
+// ------------------------------------------------------------ arguments
+
+struct AdjArgs {
+  FieldPtrs F;
+  Geom G;
+  int64_t nside, pix_begin, count;
+  const int64_t* rays;
+  int n_steps, C, nseg;
+  const float* w[6];  // map weights, indexed by ring - pix_begin
+  void* ckpt;         // [nseg + 1][state][count]
+  void* seg;          // [C][state + 57][count]
+  void* acc[4];       // padded gradient accumulators B_x, B_y, B_z, phi (NULL: not wanted)
+};
+
+template <typename T>
+__device__ __forceinline__ void store_vec(T* base, int64_t count, int64_t slot, const T* v, int n) {
+  for (int j = 0; j < n; ++j) base[(int64_t)j * count + slot] = v[j];
+}
+template <typename T>
+__device__ __forceinline__ void load_vec(const T* base, int64_t count, int64_t slot, T* v, int n) {
+  for (int j = 0; j < n; ++j) v[j] = base[(int64_t)j * count + slot];
+}
+
+// ------------------------------------------------------------ MIXED mode
+
+__global__ void __launch_bounds__(128) ckpt_kernel_mixed(const AdjArgs A) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= A.count) return;
+  const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
+  MixedRay R;
+  float y[kMixedState], x0[3];
+  mixed_observer(A.G, x0);
+  init_mixed(d, R, y);
+  float* ck = (float*)A.ckpt;
+  store_vec(ck, A.count, slot, y, kMixedState);
+#pragma unroll 1
+  for (int st = 0; st < A.n_steps; ++st) {
+    step_mixed(R, A.F, A.G, x0, st, y, nullptr);
+    const int done = st + 1;
+    if (done % A.C == 0 || done == A.n_steps) {
+      const int k = (done + A.C - 1) / A.C;
+      store_vec(ck + (int64_t)k * kMixedState * A.count, A.count, slot, y, kMixedState);
+    }
+  }
+}
+
+template <typename Acc>
+__global__ void __launch_bounds__(128) reverse_kernel_mixed(const AdjArgs A, const Acc a0, const Acc a1,
+                                                           const Acc a2, const Acc a3) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= A.count) return;
+  const Acc acc[4] = {a0, a1, a2, a3};
+  const int64_t ring = A.rays[slot];
+  const int64_t o = ring - A.pix_begin;
+  const RayDir d = ray_dir_pix(A.nside, ring);
+  MixedRay R;
+  float y[kMixedState], x0[3];
+  mixed_observer(A.G, x0);
+  init_mixed(d, R, y);
+  const float* ck = (const float*)A.ckpt;
+  float* sg = (float*)A.seg;
+  constexpr int kSeg = kMixedState + 57;
+  // cotangent of the final state from the map weights (inverse of extract_mixed)
+  float lam[19];
+  {
+    load_vec(ck + (int64_t)A.nseg * kMixedState * A.count, A.count, slot, y, kMixedState);
+    for (int j = 0; j < 19; ++j) lam[j] = 0.f;
+    float w[6];
+    for (int m = 0; m < 6; ++m) w[m] = A.w[m][o];
+    lam[12] = w[0];
+    lam[16] = w[1];
+    lam[17] = w[2];
+    lam[18] = w[3];
+    const float S = (float)A.n_steps;
+    float u[3];
+    for (int i = 0; i < 3; ++i) u[i] = (y[i] + y[19 + i]) / S;
+    const float q = R.eta[0] - 2.f * (R.n0[0] * u[0] + R.n0[1] * u[1] + R.n0[2] * u[2]) +
+                    (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    const float c = rsqrt1p_m1(q);
+    const float r3 = (1.f + c) * (1.f + c) * (1.f + c);  // (1 + q)^(-3/2)
+    float Db[3], um[3];
+    for (int i = 0; i < 3; ++i) {
+      Db[i] = w[4] * R.a0[i] + w[5] * R.b0[i];
+      um[i] = u[i] - R.n0[i];
+    }
+    const float dotv = um[0] * Db[0] + um[1] * Db[1] + um[2] * Db[2];
+    for (int i = 0; i < 3; ++i) lam[i] = ((1.f + c) * Db[i] - dotv * r3 * um[i]) / S;
+  }
+#pragma unroll 1
+  for (int sgi = A.nseg - 1; sgi >= 0; --sgi) {
+    const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
+    load_vec(ck + (int64_t)sgi * kMixedState * A.count, A.count, slot, y, kMixedState);
+#pragma unroll 1
+    for (int st = s0; st < s1; ++st) {
+      float* rec = sg + (int64_t)(st - s0) * kSeg * A.count;
+      store_vec(rec, A.count, slot, y, kMixedState);
+      float ks[57];
+      step_mixed(R, A.F, A.G, x0, st, y, ks);
+      store_vec(rec + (int64_t)kMixedState * A.count, A.count, slot, ks, 57);
+    }
+#pragma unroll 1
+    for (int st = s1 - 1; st >= s0; --st) {
+      const float* rec = sg + (int64_t)(st - s0) * kSeg * A.count;
+      float yi[kMixedState];
+      load_vec(rec, A.count, slot, yi, kMixedState);
+      float anext[19], atot[19];
+      for (int j = 0; j < 19; ++j) atot[j] = 0.f;
+#pragma unroll 1
+      for (int stage = 3; stage >= 0; --stage) {
+        // stage input u = y + c k_prev, c = 0, 1/2, 1/2, 1
+        float kprev[19], u[19], fb[19];
+        const float c = (stage == 0) ? 0.f : ((stage == 3) ? 1.f : 0.5f);
+        if (stage == 0) {
+          for (int j = 0; j < 19; ++j) kprev[j] = 0.f;
+        } else {
+          load_vec(rec + (int64_t)(kMixedState + 19 * (stage - 1)) * A.count, A.count, slot, kprev, 19);
+        }
+        mixed_stage(yi, kprev, c, u);
+        // output cotangent of this stage's k
+        const float wl = (stage == 0 || stage == 3) ? (1.f / 6.f) : (1.f / 3.f);
+        const float wa = (stage == 3) ? 0.f : ((stage == 2) ? 1.f : 0.5f);
+        for (int j = 0; j < 19; ++j) fb[j] = wl * lam[j] + (stage == 3 ? 0.f : wa * anext[j]);
+        StageView<float> V;
+        stage_view_mixed(u, (float)st + c, R, A.G, x0, V);
+        float ub[19];
+        for (int j = 0; j < 19; ++j) ub[j] = 0.f;
+        rhs_vjp<float, Acc>(V, A.F, A.G, fb, ub, acc);
+        for (int j = 0; j < 19; ++j) {
+          anext[j] = ub[j];
+          atot[j] += ub[j];
+        }
+      }
+      for (int j = 0; j < 19; ++j) lam[j] += atot[j];
+    }
+  }
+}
+
+// ------------------------------------------------------------- FP64 mode
+
+__global__ void __launch_bounds__(128) ckpt_kernel_fp64(const AdjArgs A) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= A.count) return;
+  const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
+  double y[19];
+  init_std(d, A.G, y);
+  double* ck = (double*)A.ckpt;
+  store_vec(ck, A.count, slot, y, 19);
+#pragma unroll 1
+  for (int st = 0; st < A.n_steps; ++st) {
+    step_std<kFP64>(A.F, A.G, y, nullptr);
+    const int done = st + 1;
+    if (done % A.C == 0 || done == A.n_steps) {
+      const int k = (done + A.C - 1) / A.C;
+      store_vec(ck + (int64_t)k * 19 * A.count, A.count, slot, y, 19);
+    }
+  }
+}
+
+template <typename Acc>
+__global__ void __launch_bounds__(128) reverse_kernel_fp64(const AdjArgs A, const Acc a0, const Acc a1,
+                                                          const Acc a2, const Acc a3) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= A.count) return;
+  const Acc acc[4] = {a0, a1, a2, a3};
+  const int64_t ring = A.rays[slot];
+  const int64_t o = ring - A.pix_begin;
+  const RayDir d = ray_dir_pix(A.nside, ring);
+  const double* ck = (const double*)A.ckpt;
+  double* sg = (double*)A.seg;
+  constexpr int kSeg = 19 + 57;
+  double y[19], lam[19];
+  {
+    load_vec(ck + (int64_t)A.nseg * 19 * A.count, A.count, slot, y, 19);
+    for (int j = 0; j < 19; ++j) lam[j] = 0.0;
+    double w[6];
+    for (int m = 0; m < 6; ++m) w[m] = A.w[m][o];
+    lam[12] = w[0];
+    lam[16] = w[1];
+    lam[17] = w[2];
+    lam[18] = w[3];
+    // deflection = (X/|X| - r_hat) . (e_theta, e2): Xb = (I - X^ X^T) Db / |X|
+    double X[3];
+    for (int i = 0; i < 3; ++i) X[i] = y[i] - (double)A.G.n[i] * 0.5;
+    const double nrm = sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]);
+    const double Db[3] = {w[4] * d.ct * d.cp + w[5] * d.sp, w[4] * d.ct * d.sp - w[5] * d.cp, -w[4] * d.st};
+    const double xd = (X[0] * Db[0] + X[1] * Db[1] + X[2] * Db[2]) / nrm;
+    for (int i = 0; i < 3; ++i) lam[i] = (Db[i] - X[i] / nrm * xd) / nrm;
+  }
+#pragma unroll 1
+  for (int sgi = A.nseg - 1; sgi >= 0; --sgi) {
+    const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
+    load_vec(ck + (int64_t)sgi * 19 * A.count, A.count, slot, y, 19);
+#pragma unroll 1
+    for (int st = s0; st < s1; ++st) {
+      double* rec = sg + (int64_t)(st - s0) * kSeg * A.count;
+      store_vec(rec, A.count, slot, y, 19);
+      double ks[57];
+      step_std<kFP64>(A.F, A.G, y, ks);
+      store_vec(rec + (int64_t)19 * A.count, A.count, slot, ks, 57);
+    }
+#pragma unroll 1
+    for (int st = s1 - 1; st >= s0; --st) {
+      const double* rec = sg + (int64_t)(st - s0) * kSeg * A.count;
+      double yi[19], anext[19], atot[19];
+      load_vec(rec, A.count, slot, yi, 19);
+      for (int j = 0; j < 19; ++j) atot[j] = 0.0;
+#pragma unroll 1
+      for (int stage = 3; stage >= 0; --stage) {
+        double u[19], fb[19];
+        const double c = (stage == 0) ? 0.0 : ((stage == 3) ? 1.0 : 0.5);
+        if (stage == 0) {
+          for (int j = 0; j < 19; ++j) u[j] = yi[j];
+        } else {
+          double kprev[19];
+          load_vec(rec + (int64_t)(19 + 19 * (stage - 1)) * A.count, A.count, slot, kprev, 19);
+          for (int j = 0; j < 19; ++j) u[j] = yi[j] + c * kprev[j];
+        }
+        const double wl = (stage == 0 || stage == 3) ? (1.0 / 6.0) : (1.0 / 3.0);
+        const double wa = (stage == 3) ? 0.0 : ((stage == 2) ? 1.0 : 0.5);
+        for (int j = 0; j < 19; ++j) fb[j] = wl * lam[j] + (stage == 3 ? 0.0 : wa * anext[j]);
+        StageView<double> V;
+        stage_view_fp64(u, A.G, V);
+        double ub[19];
+        for (int j = 0; j < 19; ++j) ub[j] = 0.0;
+        rhs_vjp<double, Acc>(V, A.F, A.G, fb, ub, acc);
+        for (int j = 0; j < 19; ++j) {
+          anext[j] = ub[j];
+          atot[j] += ub[j];
+        }
+      }
+      for (int j = 0; j < 19; ++j) lam[j] += atot[j];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ fold
+
+template <typename G>
+__device__ __forceinline__ double fold_value(G v) { return (double)v; }
+template <>
+__device__ __forceinline__ double fold_value<unsigned long long>(unsigned long long v) {
+  return (double)(long long)v / kFixedScale;
+}
+
+// For voxel (i, j, k): sum of the padded copies (the interior one and the
+// halo copies) -> out[v * stride + comp] (+= when accumulate).
+template <typename G>
+__global__ void fold_kernel(const G* __restrict__ padded, int64_t n0, int64_t n1, int64_t n2, float* out, int stride,
+                            int comp, int accumulate) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n0 * n1 * n2) return;
+  const int64_t i = v % n0, j = (v / n0) % n1, k = v / (n0 * n1);
+  const int64_t p0 = n0 + 3, p1 = n1 + 3;
+  int64_t pi[4], pj[4], pk[4];
+  int ni = 0, nj = 0, nk = 0;
+  // padded coordinate q maps to voxel (q - 1) mod n for q in [0, n + 3)
+  pi[ni++] = i + 1;
+  if (i == n0 - 1) pi[ni++] = 0;
+  if (i == 0) pi[ni++] = n0 + 1;
+  if (i == 1 % n0) pi[ni++] = n0 + 2;
+  pj[nj++] = j + 1;
+  if (j == n1 - 1) pj[nj++] = 0;
+  if (j == 0) pj[nj++] = n1 + 1;
+  if (j == 1 % n1) pj[nj++] = n1 + 2;
+  pk[nk++] = k + 1;
+  if (k == n2 - 1) pk[nk++] = 0;
+  if (k == 0) pk[nk++] = n2 + 1;
+  if (k == 1 % n2) pk[nk++] = n2 + 2;
+  G sum = 0;
+  for (int a = 0; a < nk; ++a)
+    for (int b = 0; b < nj; ++b)
+      for (int c = 0; c < ni; ++c) sum += padded[pi[c] + p0 * (pj[b] + p1 * pk[a])];
+  const float val = (float)fold_value<G>(sum);
+  float* dst = out + v * stride + comp;
+  *dst = accumulate ? *dst + val : val;
+}
+
+}  // namespace srt
+
+using namespace srt;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 1); }
+};
+
+template <typename Acc, typename E>
+void make_acc(Acc* acc, void* const* bufs) {
+  for (int f = 0; f < 4; ++f) acc[f].g = (E*)bufs[f];
+}
+
+}  // namespace
+
+#define VJP_TRY(expr, what)          \
+  do {                               \
+    cudaError_t _e = (expr);         \
+    if (_e != cudaSuccess) {         \
+      rc = cuda_error(_e, what);     \
+      goto done;                     \
+    }                                \
+  } while (0)
+
+extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
+                       int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz,
+                       int ckpt_every, unsigned flags, void* stream, srt_stats* stats) {
+  const auto t_wall = std::chrono::steady_clock::now();
+  if (!fields) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: fields is NULL");
+  if (nside < 1 || nside > (int64_t(1) << 16))
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: invalid nside %lld", (long long)nside);
+  const int64_t npix = 12 * nside * nside;
+  if (pix_begin < 0 || pix_count < 0 || pix_begin > npix || pix_count > npix - pix_begin)
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: pixel range outside [0, %lld)", (long long)npix);
+  if (n_steps < 1 || n_steps > (1 << 22)) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: invalid n_steps %d", n_steps);
+  if (precision != SRT_PRECISION_FP64 && precision != SRT_PRECISION_MIXED)
+    return set_error(precision == SRT_PRECISION_REF16 ? SRT_ERR_UNSUPPORTED : SRT_ERR_INVALID_ARGUMENT,
+                     "srt_vjp: precision %d has no adjoint (use SRT_PRECISION_FP64 or SRT_PRECISION_MIXED)", precision);
+  if (!weights) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: weights is NULL");
+  for (int m = 0; m < 6; ++m)
+    if (!weights[m] && pix_count > 0) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: weights[%d] is NULL", m);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  const srt_fields* f = fields;
+  const int64_t vox = f->n[0] * f->n[1] * f->n[2];
+  const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
+  const bool dev_io = (flags & SRT_OUTPUT_DEVICE) != 0;
+  const bool accumulate = (flags & SRT_ACCUMULATE) != 0;
+  const bool determ = (flags & SRT_DETERMINISTIC) != 0;
+  const bool fp64 = precision == SRT_PRECISION_FP64;
+  cudaStream_t s = (cudaStream_t)stream;
+  int C = ckpt_every > 0 ? ckpt_every : (int)std::max(1.0, std::floor(std::sqrt((double)n_steps) + 0.5));
+  if (C > n_steps) C = n_steps;
+  const int nseg = (n_steps + C - 1) / C;
+  int rc = SRT_OK;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (prev != f->device) cudaSetDevice(f->device);
+  DevBuf counts, offsets, rays, wdev, ckpt, seg, gacc[4], gout_phi, gout_b;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int64_t kernels = 0, h2d = 0, d2h = 0;
+  {
+    const size_t accsz = (determ || fp64) ? 8 : 4;
+    if (!dev_io) {
+      // host gradients: start from zero (or from the caller's values when accumulating)
+      if (dphi) {
+        VJP_TRY(gout_phi.alloc(vox * sizeof(float)), "cudaMalloc(dphi)");
+        if (accumulate) {
+          VJP_TRY(cudaMemcpyAsync(gout_phi.p, dphi, vox * sizeof(float), cudaMemcpyHostToDevice, s), "copy dphi");
+          h2d += vox * sizeof(float);
+        }
+      }
+      if (db_xyz) {
+        VJP_TRY(gout_b.alloc(3 * vox * sizeof(float)), "cudaMalloc(db)");
+        if (accumulate) {
+          VJP_TRY(cudaMemcpyAsync(gout_b.p, db_xyz, 3 * vox * sizeof(float), cudaMemcpyHostToDevice, s), "copy db");
+          h2d += 3 * vox * sizeof(float);
+        }
+      }
+    }
+    float* out_phi = dev_io ? dphi : (float*)gout_phi.p;
+    float* out_b = dev_io ? db_xyz : (float*)gout_b.p;
+    if (pix_count > 0 && (dphi || db_xyz)) {
+      // ---- ray list
+      RangeArgs ra;
+      ra.nside = nside;
+      int l = 0;
+      while ((int64_t(1) << l) < nside) ++l;
+      ra.log2p = l;
+      ra.launch_rays = 12 * (int64_t(1) << (2 * l));
+      ra.pix_begin = pix_begin;
+      ra.pix_count = pix_count;
+      const int64_t nblk = (ra.launch_rays + kListBlock - 1) / kListBlock;
+      VJP_TRY(counts.alloc(nblk * sizeof(int)), "cudaMalloc(ray counts)");
+      VJP_TRY(offsets.alloc(nblk * sizeof(int64_t)), "cudaMalloc(ray offsets)");
+      VJP_TRY(rays.alloc(pix_count * sizeof(int64_t)), "cudaMalloc(ray list)");
+      ray_count_kernel<<<(unsigned)nblk, kListBlock, 0, s>>>(ra, (int*)counts.p);
+      ++kernels;
+      VJP_TRY(cudaGetLastError(), "ray_count_kernel");
+      std::vector<int> hc(nblk);
+      std::vector<int64_t> ho(nblk);
+      VJP_TRY(cudaMemcpyAsync(hc.data(), counts.p, nblk * sizeof(int), cudaMemcpyDeviceToHost, s), "copy counts");
+      VJP_TRY(cudaStreamSynchronize(s), "ray count");
+      int64_t run = 0;
+      for (int64_t b = 0; b < nblk; ++b) {
+        ho[b] = run;
+        run += hc[b];
+      }
+      if (run != pix_count) {
+        rc = set_error(SRT_ERR_CUDA, "srt_vjp: ray list has %lld rays, expected %lld", (long long)run,
+                       (long long)pix_count);
+        goto done;
+      }
+      VJP_TRY(cudaMemcpyAsync(offsets.p, ho.data(), nblk * sizeof(int64_t), cudaMemcpyHostToDevice, s), "copy offsets");
+      ray_write_kernel<<<(unsigned)nblk, kListBlock, 0, s>>>(ra, (const int64_t*)offsets.p, (int64_t*)rays.p);
+      ++kernels;
+      VJP_TRY(cudaGetLastError(), "ray_write_kernel");
+
+      // ---- weights on the device
+      const float* wd[6];
+      if (dev_io) {
+        for (int m = 0; m < 6; ++m) wd[m] = weights[m];
+      } else {
+        VJP_TRY(wdev.alloc(6 * pix_count * sizeof(float)), "cudaMalloc(weights)");
+        for (int m = 0; m < 6; ++m) {
+          VJP_TRY(cudaMemcpyAsync((float*)wdev.p + m * pix_count, weights[m], pix_count * sizeof(float),
+                                  cudaMemcpyHostToDevice, s),
+                  "copy weights");
+          wd[m] = (const float*)wdev.p + m * pix_count;
+        }
+        h2d += 6 * pix_count * (int64_t)sizeof(float);
+      }
+
+      // ---- scratch: checkpoints, segment records, padded accumulators
+      const int state = fp64 ? 19 : kMixedState;
+      const size_t esz = fp64 ? sizeof(double) : sizeof(float);
+      VJP_TRY(ckpt.alloc((size_t)(nseg + 1) * state * pix_count * esz), "cudaMalloc(checkpoints)");
+      VJP_TRY(seg.alloc((size_t)C * (state + 57) * pix_count * esz), "cudaMalloc(segment records)");
+      for (int fld = 0; fld < 4; ++fld) {
+        const bool want = (fld == 3) ? (dphi != nullptr) : (db_xyz != nullptr);
+        if (!want) continue;
+        VJP_TRY(gacc[fld].alloc(pvox * accsz), "cudaMalloc(gradient accumulators)");
+        VJP_TRY(cudaMemsetAsync(gacc[fld].p, 0, pvox * accsz, s), "clear accumulators");
+      }
+
+      AdjArgs A;
+      A.F = make_ptrs(f);
+      A.G = make_geom(f);
+      A.nside = nside;
+      A.pix_begin = pix_begin;
+      A.count = pix_count;
+      A.rays = (const int64_t*)rays.p;
+      A.n_steps = n_steps;
+      A.C = C;
+      A.nseg = nseg;
+      for (int m = 0; m < 6; ++m) A.w[m] = wd[m];
+      A.ckpt = ckpt.p;
+      A.seg = seg.p;
+      for (int fld = 0; fld < 4; ++fld) A.acc[fld] = gacc[fld].p;
+
+      VJP_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+      VJP_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+      VJP_TRY(cudaEventRecord(e0, s), "cudaEventRecord");
+      const unsigned blocks = (unsigned)((pix_count + 127) / 128);
+      if (fp64) {
+        ckpt_kernel_fp64<<<blocks, 128, 0, s>>>(A);
+        if (determ) {
+          AccFixed ac[4];
+          make_acc<AccFixed, unsigned long long>(ac, A.acc);
+          reverse_kernel_fp64<AccFixed><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
+        } else {
+          AccF64 ac[4];
+          make_acc<AccF64, double>(ac, A.acc);
+          reverse_kernel_fp64<AccF64><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
+        }
+      } else {
+        ckpt_kernel_mixed<<<blocks, 128, 0, s>>>(A);
+        if (determ) {
+          AccFixed ac[4];
+          make_acc<AccFixed, unsigned long long>(ac, A.acc);
+          reverse_kernel_mixed<AccFixed><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
+        } else {
+          AccF32 ac[4];
+          make_acc<AccF32, float>(ac, A.acc);
+          reverse_kernel_mixed<AccF32><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
+        }
+      }
+      kernels += 2;
+      VJP_TRY(cudaGetLastError(), "adjoint kernels");
+      // ---- fold onto the periodic grid
+      const unsigned fblocks = (unsigned)((vox + 255) / 256);
+      for (int fld = 0; fld < 4; ++fld) {
+        if (!gacc[fld].p) continue;
+        float* dst = (fld == 3) ? out_phi : out_b;
+        const int stride = (fld == 3) ? 1 : 3, comp = (fld == 3) ? 0 : fld;
+        const int accum = accumulate ? 1 : 0;
+        if (determ)
+          fold_kernel<unsigned long long><<<fblocks, 256, 0, s>>>((const unsigned long long*)gacc[fld].p, f->n[0],
+                                                                 f->n[1], f->n[2], dst, stride, comp, accum);
+        else if (fp64)
+          fold_kernel<double><<<fblocks, 256, 0, s>>>((const double*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
+                                                     stride, comp, accum);
+        else
+          fold_kernel<float><<<fblocks, 256, 0, s>>>((const float*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
+                                                    stride, comp, accum);
+        ++kernels;
+      }
+      VJP_TRY(cudaGetLastError(), "fold kernel");
+      VJP_TRY(cudaEventRecord(e1, s), "cudaEventRecord");
+    } else if (!accumulate) {
+      if (out_phi) VJP_TRY(cudaMemsetAsync(out_phi, 0, vox * sizeof(float), s), "clear dphi");
+      if (out_b) VJP_TRY(cudaMemsetAsync(out_b, 0, 3 * vox * sizeof(float), s), "clear db");
+    }
+    if (!dev_io) {
+      if (dphi) {
+        VJP_TRY(cudaMemcpyAsync(dphi, out_phi, vox * sizeof(float), cudaMemcpyDeviceToHost, s), "copy dphi back");
+        d2h += vox * sizeof(float);
+      }
+      if (db_xyz) {
+        VJP_TRY(cudaMemcpyAsync(db_xyz, out_b, 3 * vox * sizeof(float), cudaMemcpyDeviceToHost, s), "copy db back");
+        d2h += 3 * vox * sizeof(float);
+      }
+    }
+    VJP_TRY(cudaStreamSynchronize(s), "srt_vjp");
+    if (stats) {
+      float ms = -1.f;
+      if (e0 && e1) cudaEventElapsedTime(&ms, e0, e1);
+      stats->trace_ms = ms;
+      stats->rays = pix_count;
+      stats->ray_steps = pix_count * (int64_t)n_steps;
+      stats->kernels = kernels;
+      stats->h2d_bytes = h2d;
+      stats->d2h_bytes = d2h;
+    }
+  }
+done:
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (prev != f->device) cudaSetDevice(prev);
+  if (stats)
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall).count();
+  return rc;
+}

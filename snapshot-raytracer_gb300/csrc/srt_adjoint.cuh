@@ -1,0 +1,474 @@
+// srt_adjoint.cuh — reverse mode (vector-Jacobian product) of one evaluation of
+// the tracer's right-hand side (snapshot-raytracer.cu:315-510), for the vjp of
+// the maps with respect to the phi and B grids.
+//
+// The reverse sweep of an RK4 step (snapshot-raytracer.cu:524-549) needs, for
+// each stage input u and output cotangent fb, ub = J(u)^T fb together with the
+// cotangents of the grid values the stage read. Derived by hand from the
+// forward computation in srt_scheme.cuh:
+//   * every intermediate cotangent of the right-hand side (of L = n.g + n.ngB/4,
+//     of P_perp:H, of the shear projections S1/S2, of the tidal matrix T, of
+//     n.lap B, n.grad B and the e.n.grad B scalars, of phi, grad phi, Hess phi
+//     and of the B values) depends on fb and on the state only, so each field's
+//     cotangent (value, gradient, Hessian) is known before the field is read;
+//   * one fused pass per field then interpolates value, gradient, Hessian and
+//     the ten third derivatives (the position cotangent needs d/dx of the
+//     Hessian), scatters the 64 tap cotangents into the gradient grid, and
+//     adds the field's share of the state cotangents;
+//   * the terms that need sums over fields (v = 2g + n.grad B, L, P_perp:H,
+//     the effective tidal matrix) are added after the four passes.
+// Catmull-Rom's third derivative is piecewise constant: weights (-3, 9, -9, 3).
+#pragma once
+#include "srt_scheme.cuh"
+
+namespace srt {
+
+template <typename T>
+struct CRW4 {  // Catmull-Rom weights for value and d/dt .. d3/dt3
+  T w[4], g[4], h[4], k[4];
+};
+
+template <typename T>
+SRT_HD void cr_weights4(T t, CRW4<T>& c) {
+  CRW<T> b;
+  cr_weights(t, b);
+  for (int i = 0; i < 4; ++i) {
+    c.w[i] = b.w[i];
+    c.g[i] = b.g[i];
+    c.h[i] = b.h[i];
+  }
+  c.k[0] = T(-3);
+  c.k[1] = T(9);
+  c.k[2] = T(-9);
+  c.k[3] = T(3);
+}
+
+// ---------------------------------------------------------- accumulators
+
+// Where the tap cotangents go: a halo-padded gradient grid (same indexing as
+// the padded field). Three flavours: FP32 atomics, FP64 atomics, and 64-bit
+// fixed point (order-independent, so repeated runs give identical bits).
+// A null grid (gradient not requested) ignores the contributions.
+struct AccF32 {
+  float* g;
+  SRT_HD void add(int64_t i, float v) const {
+    if (!g) return;
+#if defined(__CUDA_ARCH__)
+    atomicAdd(g + i, v);
+#else
+    g[i] += v;
+#endif
+  }
+};
+
+struct AccF64 {
+  double* g;
+  SRT_HD void add(int64_t i, double v) const {
+    if (!g) return;
+#if defined(__CUDA_ARCH__)
+    atomicAdd(g + i, v);
+#else
+    g[i] += v;
+#endif
+  }
+};
+
+// Fixed point with kFixedScale = 2^32 units per unit of gradient; |gradient|
+// per voxel must stay below 2^31. Contributions are rounded to the nearest
+// unit before the integer addition, so the result does not depend on the
+// order of the additions.
+constexpr double kFixedScale = 4294967296.0;
+
+struct AccFixed {
+  unsigned long long* g;
+  SRT_HD void add(int64_t i, double v) const {
+    if (!g) return;
+    const long long q = llrint(v * kFixedScale);
+#if defined(__CUDA_ARCH__)
+    atomicAdd(g + i, (unsigned long long)q);
+#else
+    g[i] += (unsigned long long)q;
+#endif
+  }
+};
+
+// ------------------------------------------------- fused field pass (vjp)
+
+// Interpolates one field (value, gradient, Hessian into Q; third derivatives
+// used internally), adds qb . dQ/dposition to xb and scatters the cotangent of
+// every tap, sum_q qb_q W_q(tap), through `acc`.
+// qb: cotangents of (v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz); the
+// Hessian entries are the unique components (off-diagonal cotangents already
+// hold both symmetric halves).
+template <typename T, typename Acc>
+SRT_HD void tricubic_vjp(const float* __restrict__ f, int64_t base, int64_t px, int64_t pxy, T tx, T ty, T tz,
+                         const T* qb, Tri<T>& Q, T* xb, const Acc& acc) {
+  CRW4<T> X, Y, Z;
+  cr_weights4(tx, X);
+  cr_weights4(ty, Y);
+  cr_weights4(tz, Z);
+  // per-row scatter factors: the tap cotangent of row (b, c) is
+  // wx_i Cw + gx_i Cg + hx_i Ch with Cw = wz_c Aw_b + gz_c Bw_b + hz_c Dw_b,
+  // Cg = wz_c Ag_b + gz_c Bg_b, Ch = wz_c Ah_b.
+  T Aw[4], Bw[4], Dw[4], Ag[4], Bg[4], Ah[4];
+  for (int b = 0; b < 4; ++b) {
+    Aw[b] = qb[0] * Y.w[b] + qb[2] * Y.g[b] + qb[7] * Y.h[b];
+    Bw[b] = qb[3] * Y.w[b] + qb[8] * Y.g[b];
+    Dw[b] = qb[9] * Y.w[b];
+    Ag[b] = qb[1] * Y.w[b] + qb[5] * Y.g[b];
+    Bg[b] = qb[6] * Y.w[b];
+    Ah[b] = qb[4] * Y.w[b];
+  }
+  // 20 accumulators: derivative orders (x, y, z) with x + y + z <= 3
+  T o000 = 0, o001 = 0, o002 = 0, o003 = 0, o010 = 0, o011 = 0, o012 = 0, o020 = 0, o021 = 0, o030 = 0;
+  T o100 = 0, o101 = 0, o102 = 0, o110 = 0, o111 = 0, o120 = 0, o200 = 0, o201 = 0, o210 = 0, o300 = 0;
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c) {
+    T s00 = 0, s01 = 0, s02 = 0, s03 = 0, s10 = 0, s11 = 0, s12 = 0, s20 = 0, s21 = 0, s30 = 0;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t row = base + c * pxy + b * px;
+      const float* rp = f + row;
+      const T p0 = (T)ldg(rp), p1 = (T)ldg(rp + 1), p2 = (T)ldg(rp + 2), p3 = (T)ldg(rp + 3);
+      const T r0 = X.w[0] * p0 + X.w[1] * p1 + X.w[2] * p2 + X.w[3] * p3;
+      const T r1 = X.g[0] * p0 + X.g[1] * p1 + X.g[2] * p2 + X.g[3] * p3;
+      const T r2 = X.h[0] * p0 + X.h[1] * p1 + X.h[2] * p2 + X.h[3] * p3;
+      const T r3 = X.k[0] * p0 + X.k[1] * p1 + X.k[2] * p2 + X.k[3] * p3;
+      s00 += Y.w[b] * r0;
+      s01 += Y.g[b] * r0;
+      s02 += Y.h[b] * r0;
+      s03 += Y.k[b] * r0;
+      s10 += Y.w[b] * r1;
+      s11 += Y.g[b] * r1;
+      s12 += Y.h[b] * r1;
+      s20 += Y.w[b] * r2;
+      s21 += Y.g[b] * r2;
+      s30 += Y.w[b] * r3;
+      const T Cw = Z.w[c] * Aw[b] + Z.g[c] * Bw[b] + Z.h[c] * Dw[b];
+      const T Cg = Z.w[c] * Ag[b] + Z.g[c] * Bg[b];
+      const T Ch = Z.w[c] * Ah[b];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc.add(row + i, X.w[i] * Cw + X.g[i] * Cg + X.h[i] * Ch);
+    }
+    const T zw = Z.w[c], zg = Z.g[c], zh = Z.h[c], zk = Z.k[c];
+    o000 += zw * s00; o001 += zg * s00; o002 += zh * s00; o003 += zk * s00;
+    o010 += zw * s01; o011 += zg * s01; o012 += zh * s01;
+    o020 += zw * s02; o021 += zg * s02;
+    o030 += zw * s03;
+    o100 += zw * s10; o101 += zg * s10; o102 += zh * s10;
+    o110 += zw * s11; o111 += zg * s11;
+    o120 += zw * s12;
+    o200 += zw * s20; o201 += zg * s20;
+    o210 += zw * s21;
+    o300 += zw * s30;
+  }
+  Q.v = o000;
+  Q.g[0] = o100;
+  Q.g[1] = o010;
+  Q.g[2] = o001;
+  Q.h[0] = o200;
+  Q.h[1] = o110;
+  Q.h[2] = o101;
+  Q.h[3] = o020;
+  Q.h[4] = o011;
+  Q.h[5] = o002;
+  // xb_j += qb . dQ/dx_j
+  xb[0] += qb[0] * o100 + qb[1] * o200 + qb[2] * o110 + qb[3] * o101 + qb[4] * o300 + qb[5] * o210 +
+           qb[6] * o201 + qb[7] * o120 + qb[8] * o111 + qb[9] * o102;
+  xb[1] += qb[0] * o010 + qb[1] * o110 + qb[2] * o020 + qb[3] * o011 + qb[4] * o210 + qb[5] * o120 +
+           qb[6] * o111 + qb[7] * o030 + qb[8] * o021 + qb[9] * o012;
+  xb[2] += qb[0] * o001 + qb[1] * o101 + qb[2] * o011 + qb[3] * o002 + qb[4] * o201 + qb[5] * o111 +
+           qb[6] * o102 + qb[7] * o021 + qb[8] * o012 + qb[9] * o003;
+}
+
+// -------------------------------------------------------- stage and core
+
+// What the right-hand-side vjp needs about one stage input, independent of
+// the state representation (FP64 full state or MIXED perturbation state).
+template <typename T>
+struct StageView {
+  T n[3], a[3], b[3];  // unit vectors n, e1, e2
+  T rn, ra, rb;        // 1 / |raw vector| (normalisation Jacobians)
+  T A, Ap, s1, s2, e1, e2;
+  bool branch;         // dA > 1/2
+  int64_t base[4];     // padded base index per field: B_x, B_y, B_z, phi
+  T t[4][3];           // cell offsets per field and axis
+};
+
+// symmetric 3x3 as unique components xx xy xz yy yz zz
+SRT_HD int sym_idx(int i, int j) {
+  return (i == j) ? (i == 0 ? 0 : (i == 1 ? 3 : 5)) : ((i + j == 1) ? 1 : ((i + j == 2) ? 2 : 4));
+}
+
+template <typename T>
+SRT_HD T symv(const T* h, int i, int j) { return h[sym_idx(i, j)]; }
+
+// yb += J(u)^T fb for the stage described by V; tap cotangents go to acc[0..3]
+// (B_x, B_y, B_z, phi).
+template <typename T, typename Acc>
+SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, const T* fb, T* yb, const Acc* acc) {
+  const T* n = V.n;
+  const T* a = V.a;
+  const T* b = V.b;
+  // ---- intermediate cotangents (state only)
+  const T nfx = n[0] * fb[0] + n[1] * fb[1] + n[2] * fb[2];
+  const T nfn = n[0] * fb[3] + n[1] * fb[4] + n[2] * fb[5];
+  const T sab = -(n[0] * fb[6] + n[1] * fb[7] + n[2] * fb[8]);
+  const T sbb = -(n[0] * fb[9] + n[1] * fb[10] + n[2] * fb[11]);
+  const T phib = T(-2) * nfx;
+  T vb[3];
+  for (int i = 0; i < 3; ++i) vb[i] = fb[3 + i] - n[i] * nfn;
+  const T agb = T(2) * sab, bgb = T(2) * sbb, e1b = sab, e2b = sbb;
+  T Apb = -fb[12];
+  const T Lb = T(-4) * V.Ap * fb[13] + T(4) * V.s1 * fb[14] + T(4) * V.s2 * fb[15];
+  const T PHb = -V.A * fb[13];
+  const T nlapb = T(0.5) * V.A * fb[13];
+  const T S1b = V.A * V.A * fb[14], S2b = V.A * V.A * fb[15];
+  T Ab = 0, s1b = 0, s2b = 0, el1b = 0, el2b = 0;
+  if (V.branch) {
+    const T A2 = V.A * V.A, A3 = A2 * V.A;
+    const T q = sqrt(T(4) + V.e1 * V.e1 + V.e2 * V.e2);
+    s1b += T(2) * V.s1 / A3 * fb[13];
+    s2b += T(2) * V.s2 / A3 * fb[13];
+    Ab += T(-3) * (V.s1 * V.s1 + V.s2 * V.s2) / (A3 * V.A) * fb[13];
+    s1b += T(-2) * q / A2 * fb[16];
+    T qb = T(-2) * V.s1 / A2 * fb[16];
+    Ab += T(4) * V.s1 * q / A3 * fb[16];
+    s2b += T(-2) * q / A2 * fb[17];
+    qb += T(-2) * V.s2 / A2 * fb[17];
+    Ab += T(4) * V.s2 * q / A3 * fb[17];
+    const T D = A2 * (T(2) + q), N = V.s1 * V.e2 - V.s2 * V.e1;
+    const T Nb = -fb[18] / D, Db = N * fb[18] / (D * D);
+    s1b += V.e2 * Nb;
+    el2b += V.s1 * Nb;
+    s2b += -V.e1 * Nb;
+    el1b += -V.s2 * Nb;
+    Ab += T(2) * V.A * (T(2) + q) * Db;
+    qb += A2 * Db;
+    el1b += V.e1 / q * qb;
+    el2b += V.e2 / q * qb;
+  }
+  // cotangent of the effective tidal matrix He = H + T/2 (full symmetric)
+  T Heb[6];
+  for (int i = 0; i < 3; ++i)
+    for (int j = i; j < 3; ++j)
+      Heb[sym_idx(i, j)] = (a[i] * a[j] - b[i] * b[j]) * S1b + (a[i] * b[j] + b[i] * a[j]) * S2b;
+  T Tb[6];
+  for (int u = 0; u < 6; ++u) Tb[u] = T(0.5) * Heb[u];
+  T gb[3], ngBb[3];
+  for (int i = 0; i < 3; ++i) {
+    gb[i] = T(2) * vb[i] + agb * a[i] + bgb * b[i] + n[i] * Lb;
+    ngBb[i] = vb[i] + T(0.25) * n[i] * Lb;
+  }
+  T nb[3] = {0, 0, 0}, ab[3] = {0, 0, 0}, bb[3] = {0, 0, 0}, xb[3] = {0, 0, 0};
+  // aggregates of the forward
+  T ngB[3] = {0, 0, 0}, e1ngB = 0, e2ngB = 0, nlap = 0, Tm[6] = {0, 0, 0, 0, 0, 0};
+
+  // ---- B components
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    const T nc = c == 0 ? n[0] : (c == 1 ? n[1] : n[2]);
+    const T ac = c == 0 ? a[0] : (c == 1 ? a[1] : a[2]);
+    const T bc = c == 0 ? b[0] : (c == 1 ? b[1] : b[2]);
+    T qb[10];
+    qb[0] = -fb[c];
+    for (int i = 0; i < 3; ++i)
+      qb[1 + i] = nc * ngBb[i] + T(0.5) * e1b * (ac * n[i] + nc * a[i]) + T(0.5) * e2b * (bc * n[i] + nc * b[i]);
+    // Hessian cotangent: n_c Tb + n_c nlapb I - sym(e_c Tb_c. (x) n)
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j) {
+        T m = nc * symv(Tb, i, j) + ((i == j) ? nc * nlapb : T(0));
+        m -= T(0.5) * (symv(Tb, c, i) * n[j] + symv(Tb, c, j) * n[i]);
+        // unique components: off-diagonals hold both halves
+        qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
+      }
+    Tri<T> Q;
+    tricubic_vjp<T, Acc>(F.b[c], V.base[c], G.px, G.pxy, V.t[c][0], V.t[c][1], V.t[c][2], qb, Q, xb, acc[c]);
+    // forward aggregates
+    for (int i = 0; i < 3; ++i) ngB[i] += Q.g[i] * nc;
+    const T gn = Q.g[0] * n[0] + Q.g[1] * n[1] + Q.g[2] * n[2];
+    const T ga = Q.g[0] * a[0] + Q.g[1] * a[1] + Q.g[2] * a[2];
+    const T gbb = Q.g[0] * b[0] + Q.g[1] * b[1] + Q.g[2] * b[2];
+    e1ngB += T(0.5) * (ac * gn + nc * ga);
+    e2ngB += T(0.5) * (bc * gn + nc * gbb);
+    T Hn[3];
+    for (int i = 0; i < 3; ++i) Hn[i] = symv(Q.h, i, 0) * n[0] + symv(Q.h, i, 1) * n[1] + symv(Q.h, i, 2) * n[2];
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j) {
+        T d = Q.h[sym_idx(i, j)] * nc;
+        if (i == c) d -= T(0.5) * Hn[j];
+        if (j == c) d -= T(0.5) * Hn[i];
+        Tm[sym_idx(i, j)] += d;
+      }
+    const T trH = Q.h[0] + Q.h[3] + Q.h[5];
+    nlap += trH * nc;
+    // this component's share of the state cotangents
+    T HT = 0;  // H_c : Tb (full contraction)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) HT += symv(Q.h, i, j) * symv(Tb, i, j);
+    const T dnc = Q.g[0] * ngBb[0] + Q.g[1] * ngBb[1] + Q.g[2] * ngBb[2] + trH * nlapb + HT +
+                  T(0.5) * e1b * ga + T(0.5) * e2b * gbb;
+    nb[c] += dnc;
+    for (int k = 0; k < 3; ++k) {
+      T tk = 0;
+      for (int j = 0; j < 3; ++j) tk += symv(Tb, c, j) * symv(Q.h, j, k);
+      nb[k] += T(0.5) * e1b * ac * Q.g[k] + T(0.5) * e2b * bc * Q.g[k] - tk;
+      ab[k] += T(0.5) * e1b * nc * Q.g[k];
+      bb[k] += T(0.5) * e2b * nc * Q.g[k];
+    }
+    ab[c] += T(0.5) * e1b * gn;
+    bb[c] += T(0.5) * e2b * gn;
+  }
+
+  // ---- phi
+  Tri<T> P;
+  {
+    T qb[10];
+    qb[0] = phib;
+    for (int i = 0; i < 3; ++i) qb[1 + i] = gb[i];
+    for (int i = 0; i < 3; ++i)
+      for (int j = i; j < 3; ++j) {
+        const T m = Heb[sym_idx(i, j)] + (n[i] * n[j] - ((i == j) ? T(1) : T(0))) * PHb;
+        qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
+      }
+    tricubic_vjp<T, Acc>(F.phi, V.base[3], G.px, G.pxy, V.t[3][0], V.t[3][1], V.t[3][2], qb, P, xb, acc[3]);
+  }
+  const T* g = P.g;
+  for (int i = 0; i < 3; ++i) {
+    nb[i] += -(T(1) + T(2) * P.v) * fb[i];
+    ab[i] += agb * g[i];
+    bb[i] += bgb * g[i];
+    nb[i] += T(2) * PHb * (symv(P.h, i, 0) * n[0] + symv(P.h, i, 1) * n[1] + symv(P.h, i, 2) * n[2]);
+  }
+
+  // ---- terms of the field aggregates
+  T v[3];
+  for (int i = 0; i < 3; ++i) v[i] = T(2) * g[i] + ngB[i];
+  const T nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+  const T sa = T(2) * (a[0] * g[0] + a[1] * g[1] + a[2] * g[2]) + e1ngB;
+  const T sb = T(2) * (b[0] * g[0] + b[1] * g[1] + b[2] * g[2]) + e2ngB;
+  const T L = n[0] * g[0] + n[1] * g[1] + n[2] * g[2] + T(0.25) * (n[0] * ngB[0] + n[1] * ngB[1] + n[2] * ngB[2]);
+  for (int i = 0; i < 3; ++i) {
+    nb[i] += -nv * fb[3 + i] - v[i] * nfn;
+    nb[i] += -sa * fb[6 + i] - sb * fb[9 + i];
+    nb[i] += (g[i] + T(0.25) * ngB[i]) * Lb;
+  }
+  Apb += T(-4) * L * fb[13];
+  s1b += T(4) * L * fb[14];
+  s2b += T(4) * L * fb[15];
+  const T nHn = n[0] * n[0] * P.h[0] + n[1] * n[1] * P.h[3] + n[2] * n[2] * P.h[5] +
+                T(2) * (n[0] * n[1] * P.h[1] + n[0] * n[2] * P.h[2] + n[1] * n[2] * P.h[4]);
+  const T PH = nHn - (P.h[0] + P.h[3] + P.h[5]);
+  Ab += (-PH + T(0.5) * nlap) * fb[13];
+  T He[6];
+  for (int u = 0; u < 6; ++u) He[u] = P.h[u] + T(0.5) * Tm[u];
+  T Hea[3], Heb3[3];
+  for (int i = 0; i < 3; ++i) {
+    Hea[i] = symv(He, i, 0) * a[0] + symv(He, i, 1) * a[1] + symv(He, i, 2) * a[2];
+    Heb3[i] = symv(He, i, 0) * b[0] + symv(He, i, 1) * b[1] + symv(He, i, 2) * b[2];
+  }
+  const T S1 = (a[0] * Hea[0] + a[1] * Hea[1] + a[2] * Hea[2]) - (b[0] * Heb3[0] + b[1] * Heb3[1] + b[2] * Heb3[2]);
+  const T S2 = T(2) * (a[0] * Heb3[0] + a[1] * Heb3[1] + a[2] * Heb3[2]);
+  Ab += T(2) * V.A * (S1 * fb[14] + S2 * fb[15]);
+  for (int i = 0; i < 3; ++i) {
+    ab[i] += T(2) * Hea[i] * S1b + T(2) * Heb3[i] * S2b;
+    bb[i] += T(-2) * Heb3[i] * S1b + T(2) * Hea[i] * S2b;
+  }
+
+  // ---- through the normalisations, into the state cotangent
+  const T nnb = n[0] * nb[0] + n[1] * nb[1] + n[2] * nb[2];
+  const T aab = a[0] * ab[0] + a[1] * ab[1] + a[2] * ab[2];
+  const T bbb = b[0] * bb[0] + b[1] * bb[1] + b[2] * bb[2];
+  for (int i = 0; i < 3; ++i) {
+    yb[i] += xb[i];
+    yb[3 + i] += V.rn * (nb[i] - n[i] * nnb);
+    yb[6 + i] += V.ra * (ab[i] - a[i] * aab);
+    yb[9 + i] += V.rb * (bb[i] - b[i] * bbb);
+  }
+  yb[12] += Ab;
+  yb[13] += Apb;
+  yb[14] += s1b;
+  yb[15] += s2b;
+  yb[16] += el1b;
+  yb[17] += el2b;
+}
+
+// ------------------------------------------------------- stage views
+
+// FP64 full state y (layout of rhs_std).
+SRT_HD void stage_view_fp64(const double* y, const Geom& G, StageView<double>& V) {
+  const double nr = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+  const double ar = sqrt(y[6] * y[6] + y[7] * y[7] + y[8] * y[8]);
+  const double br = sqrt(y[9] * y[9] + y[10] * y[10] + y[11] * y[11]);
+  V.rn = 1.0 / nr;
+  V.ra = 1.0 / ar;
+  V.rb = 1.0 / br;
+  for (int i = 0; i < 3; ++i) {
+    V.n[i] = y[3 + i] / nr;
+    V.a[i] = y[6 + i] / ar;
+    V.b[i] = y[9 + i] / br;
+  }
+  V.A = y[12];
+  V.Ap = y[13];
+  V.s1 = y[14];
+  V.s2 = y[15];
+  V.e1 = y[16];
+  V.e2 = y[17];
+  V.branch = y[12] > 0.5;
+  for (int f = 0; f < 4; ++f) {
+    int cell[3];
+    for (int i = 0; i < 3; ++i) {
+      const double x = y[i] - ((f == i) ? 0.5 : 0.0);
+      const double fl = floor(x);
+      V.t[f][i] = x - fl;
+      cell[i] = wrap64((int64_t)fl, G.n[i]);
+    }
+    V.base[f] = cell_base(G, cell[0], cell[1], cell[2]);
+  }
+}
+
+// MIXED perturbation state d at affine parameter s (layout of rhs_mixed).
+SRT_HD void stage_view_mixed(const float* d, float s, const MixedRay& R, const Geom& G, const float* x0,
+                             StageView<float>& V) {
+  const float* v0s[3] = {R.n0, R.a0, R.b0};
+  float* outs[3] = {V.n, V.a, V.b};
+  float* rs[3] = {&V.rn, &V.ra, &V.rb};
+  for (int k = 0; k < 3; ++k) {
+    const float* v0 = v0s[k];
+    const float* dv = d + 3 + 3 * k;
+    const float q = R.eta[k] + 2.f * (v0[0] * dv[0] + v0[1] * dv[1] + v0[2] * dv[2]) +
+                    (dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    const float rm1 = rsqrt1p_m1(q);
+    *rs[k] = 1.f + rm1;
+    for (int i = 0; i < 3; ++i) outs[k][i] = v0[i] + (v0[i] * rm1 + dv[i] * (1.f + rm1));
+  }
+  V.A = s + d[12];
+  V.Ap = d[13] - 1.f;
+  V.s1 = d[14];
+  V.s2 = d[15];
+  V.e1 = d[16];
+  V.e2 = d[17];
+  V.branch = d[12] > 0.5f - s;
+  int cc[3], cs[3];
+  float tc[3], ts[3];
+  for (int i = 0; i < 3; ++i) {
+    const float p = s * R.n0[i];
+    const float pe = fmaf(s, R.n0[i], -p);
+    float th, tl;
+    two_sum(x0[i], -p, th, tl);
+    const float lo = (tl - pe) + d[i];
+    locate(th, lo, G.n[i], G.invn[i], cc[i], tc[i]);
+    locate(th - 0.5f, lo, G.n[i], G.invn[i], cs[i], ts[i]);
+  }
+  for (int f = 0; f < 4; ++f) {
+    int cell[3];
+    for (int i = 0; i < 3; ++i) {
+      const bool stag = (f == i);
+      cell[i] = stag ? cs[i] : cc[i];
+      V.t[f][i] = stag ? ts[i] : tc[i];
+    }
+    V.base[f] = cell_base(G, cell[0], cell[1], cell[2]);
+  }
+}
+
+}  // namespace srt

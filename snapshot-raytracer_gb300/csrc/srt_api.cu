@@ -285,14 +285,6 @@ fail:
   return rc;
 }
 
-int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
-            int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz, int ckpt_every,
-            unsigned flags, void* stream, srt_stats* stats) {
-  (void)fields; (void)nside; (void)pix_begin; (void)pix_count; (void)n_steps; (void)precision; (void)weights;
-  (void)dphi; (void)db_xyz; (void)ckpt_every; (void)flags; (void)stream; (void)stats;
-  return set_error(SRT_ERR_UNSUPPORTED, "srt_vjp: not available in this build");
-}
-
 int srt_pix2ang_ring(int64_t nside, int64_t pix, double* theta, double* phi) {
   if (nside < 1 || nside > (int64_t(1) << 29) || pix < 0 || pix >= 12 * nside * nside || !theta || !phi)
     return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_pix2ang_ring: bad arguments");

@@ -346,10 +346,8 @@ SRT_HD void extract_deflection(const RayDir& d, double X0, double X1, double X2,
 
 // ----------------------------------------------------- ray driver, FP64/REF16
 
-template <int MODE>
-SRT_HD void trace_ray_std(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps,
-                          float out[6]) {
-  double y[19], acc[19], k[19], ys[19];
+// Initial state of the ray (snapshot-raytracer.cu:560).
+SRT_HD void init_std(const RayDir& d, const Geom& G, double* y) {
   y[0] = (double)G.n[0] * 0.5;
   y[1] = (double)G.n[1] * 0.5;
   y[2] = (double)G.n[2] * 0.5;
@@ -365,24 +363,43 @@ SRT_HD void trace_ray_std(const FieldPtrs& F, const Geom& G, const RayDir& d, in
   y[12] = 0.0;
   y[13] = -1.0;
   for (int j = 14; j < 19; ++j) y[j] = 0.0;
+}
+
+// One RK4 step of h = 1 (snapshot-raytracer.cu:524-549); when ks is given,
+// the stage derivatives k1, k2, k3 are stored there (3 x 19).
+template <int MODE>
+SRT_HD void step_std(const FieldPtrs& F, const Geom& G, double* y, double* ks) {
+  double acc[19], k[19], ys[19];
   for (int j = 0; j < 19; ++j) k[j] = 0.0;
 #pragma unroll 1
-  for (int step = 0; step < n_steps; ++step) {
-#pragma unroll 1
-    for (int st = 0; st < 4; ++st) {
-      const double c = (st == 3) ? 1.0 : 0.5;
-      for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
-      rhs_std<MODE>(ys, k, F, G);
-      for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.0 * k[j] : acc[j]);
-    }
-    for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) / 6.0;
+  for (int st = 0; st < 4; ++st) {
+    const double c = (st == 3) ? 1.0 : 0.5;
+    for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
+    rhs_std<MODE>(ys, k, F, G);
+    if (ks && st < 3)
+      for (int j = 0; j < 19; ++j) ks[19 * st + j] = k[j];
+    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.0 * k[j] : acc[j]);
   }
+  for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) / 6.0;
+}
+
+// The six maps from the final state (snapshot-raytracer.cu:566-582).
+SRT_HD void extract_std(const RayDir& d, const Geom& G, const double* y, float out[6]) {
   out[0] = (float)y[12];
   out[1] = (float)y[16];
   out[2] = (float)y[17];
   out[3] = (float)y[18];
-  extract_deflection(d, y[0] - (double)G.n[0] * 0.5, y[1] - (double)G.n[1] * 0.5,
-                     y[2] - (double)G.n[2] * 0.5, &out[4], &out[5]);
+  extract_deflection(d, y[0] - (double)G.n[0] * 0.5, y[1] - (double)G.n[1] * 0.5, y[2] - (double)G.n[2] * 0.5,
+                     &out[4], &out[5]);
+}
+
+template <int MODE>
+SRT_HD void trace_ray_std(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6]) {
+  double y[19];
+  init_std(d, G, y);
+#pragma unroll 1
+  for (int step = 0; step < n_steps; ++step) step_std<MODE>(F, G, y, nullptr);
+  extract_std(d, G, y, out);
 }
 
 // -------------------------------------------------------------- MIXED mode
@@ -560,61 +577,77 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
 // the ray position, whose increments are ~1e-4 of its size after a few hundred
 // steps and whose error becomes the deflection error.
 constexpr int kCompensated = 3;
+// Floats of one stored MIXED state: the 19 components and the compensations.
+constexpr int kMixedState = 19 + kCompensated;
 
-SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6]) {
-  MixedRay R;
-  float yh[19], yl[kCompensated], k[19], acc[19], ys[19];
-  const float x0[3] = {(float)((double)G.n[0] * 0.5), (float)((double)G.n[1] * 0.5), (float)((double)G.n[2] * 0.5)};
-  {
-    const double n64[3] = {-d.st * d.cp, -d.st * d.sp, -d.ct};
-    const double a64[3] = {d.ct * d.cp, d.ct * d.sp, -d.st};
-    const double b64[3] = {d.sp, -d.cp, 0.0};
-    double qn = -1.0, qa = -1.0, qb = -1.0;
-    for (int i = 0; i < 3; ++i) {
-      R.n0[i] = (float)n64[i];
-      R.a0[i] = (float)a64[i];
-      R.b0[i] = (float)b64[i];
-      R.dn0[i] = (float)(n64[i] - (double)R.n0[i]);
-      yh[3 + i] = R.dn0[i];
-      yh[6 + i] = (float)(a64[i] - (double)R.a0[i]);
-      yh[9 + i] = (float)(b64[i] - (double)R.b0[i]);
-      qn += (double)R.n0[i] * (double)R.n0[i];
-      qa += (double)R.a0[i] * (double)R.a0[i];
-      qb += (double)R.b0[i] * (double)R.b0[i];
-      yh[i] = 0.f;
-    }
-    R.eta[0] = (float)qn;
-    R.eta[1] = (float)qa;
-    R.eta[2] = (float)qb;
+SRT_HD void mixed_observer(const Geom& G, float* x0) {
+  for (int i = 0; i < 3; ++i) x0[i] = (float)((double)G.n[i] * 0.5);
+}
+
+// Straight-ray bases of the ray and the initial perturbation state: y holds
+// the 19 components followed by the kCompensated compensation terms.
+SRT_HD void init_mixed(const RayDir& d, MixedRay& R, float* y) {
+  const double n64[3] = {-d.st * d.cp, -d.st * d.sp, -d.ct};
+  const double a64[3] = {d.ct * d.cp, d.ct * d.sp, -d.st};
+  const double b64[3] = {d.sp, -d.cp, 0.0};
+  double qn = -1.0, qa = -1.0, qb = -1.0;
+  for (int i = 0; i < 3; ++i) {
+    R.n0[i] = (float)n64[i];
+    R.a0[i] = (float)a64[i];
+    R.b0[i] = (float)b64[i];
+    R.dn0[i] = (float)(n64[i] - (double)R.n0[i]);
+    y[3 + i] = R.dn0[i];
+    y[6 + i] = (float)(a64[i] - (double)R.a0[i]);
+    y[9 + i] = (float)(b64[i] - (double)R.b0[i]);
+    qn += (double)R.n0[i] * (double)R.n0[i];
+    qa += (double)R.a0[i] * (double)R.a0[i];
+    qb += (double)R.b0[i] * (double)R.b0[i];
+    y[i] = 0.f;
   }
-  for (int j = 12; j < 19; ++j) yh[j] = 0.f;
-  for (int j = 0; j < kCompensated; ++j) yl[j] = 0.f;
+  R.eta[0] = (float)qn;
+  R.eta[1] = (float)qa;
+  R.eta[2] = (float)qb;
+  for (int j = 12; j < kMixedState; ++j) y[j] = 0.f;
+}
+
+// Stage input y + c k of the perturbation state (compensations folded in).
+SRT_HD void mixed_stage(const float* y, const float* k, float c, float* ys) {
+  for (int j = 0; j < kCompensated; ++j) ys[j] = y[j] + (y[19 + j] + c * k[j]);
+  for (int j = kCompensated; j < 19; ++j) ys[j] = y[j] + c * k[j];
+}
+
+// One RK4 step from affine parameter `step`; when ks is given, the stage
+// derivatives k1, k2, k3 are stored there (3 x 19).
+SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, const float* x0, int step, float* y,
+                       float* ks) {
+  float k[19], acc[19], ys[19];
   for (int j = 0; j < 19; ++j) k[j] = 0.f;
+  const float s0 = (float)step;
 #pragma unroll 1
-  for (int step = 0; step < n_steps; ++step) {
-    const float s0 = (float)step;
-#pragma unroll 1
-    for (int st = 0; st < 4; ++st) {
-      const float c = (st == 0) ? 0.f : ((st == 3) ? 1.f : 0.5f);
-      for (int j = 0; j < kCompensated; ++j) ys[j] = yh[j] + (yl[j] + c * k[j]);
-      for (int j = kCompensated; j < 19; ++j) ys[j] = yh[j] + c * k[j];
-      rhs_mixed(ys, s0 + c, R, F, G, x0, k);
-      for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
-    }
-    for (int j = 0; j < kCompensated; ++j) {
-      float sum, err;
-      two_sum(yh[j], (acc[j] + k[j]) * (1.f / 6.f), sum, err);
-      yh[j] = sum;
-      yl[j] += err;
-    }
-    for (int j = kCompensated; j < 19; ++j) yh[j] += (acc[j] + k[j]) * (1.f / 6.f);
+  for (int st = 0; st < 4; ++st) {
+    const float c = (st == 0) ? 0.f : ((st == 3) ? 1.f : 0.5f);
+    mixed_stage(y, k, c, ys);
+    rhs_mixed(ys, s0 + c, R, F, G, x0, k);
+    if (ks && st < 3)
+      for (int j = 0; j < 19; ++j) ks[19 * st + j] = k[j];
+    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
   }
-  // Extraction in FP32 on the perturbation: the displacement is
-  // X = -S n0 + dx = S (-n0 + u), u = dx / S; X/|X| - r_hat = dn0 + u (1 + c) - n0 c
-  // with c = |(-n0 + u)|^-1 - 1 and r_hat = -(n0 + dn0) (snapshot-raytracer.cu:566-582).
+  for (int j = 0; j < kCompensated; ++j) {
+    float sum, err;
+    two_sum(y[j], (acc[j] + k[j]) * (1.f / 6.f), sum, err);
+    y[j] = sum;
+    y[19 + j] += err;
+  }
+  for (int j = kCompensated; j < 19; ++j) y[j] += (acc[j] + k[j]) * (1.f / 6.f);
+}
+
+// Extraction in FP32 on the perturbation: the displacement is
+// X = -S n0 + dx = S (-n0 + u), u = dx / S; X/|X| - r_hat = dn0 + u (1 + c) - n0 c
+// with c = |(-n0 + u)|^-1 - 1 and r_hat = -(n0 + dn0) (snapshot-raytracer.cu:566-582).
+SRT_HD void extract_mixed(const MixedRay& R, int n_steps, const float* y, float out[6]) {
   const float S = (float)n_steps;
   float u[3];
-  for (int i = 0; i < 3; ++i) u[i] = (yh[i] + yl[i]) / S;
+  for (int i = 0; i < 3; ++i) u[i] = (y[i] + y[19 + i]) / S;
   const float q = R.eta[0] - 2.f * (R.n0[0] * u[0] + R.n0[1] * u[1] + R.n0[2] * u[2]) +
                   (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
   const float cc = rsqrt1p_m1(q);
@@ -623,11 +656,21 @@ SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, 
   out[4] = D[0] * R.a0[0] + D[1] * R.a0[1] + D[2] * R.a0[2];
   out[5] = D[0] * R.b0[0] + D[1] * R.b0[1] + D[2] * R.b0[2];
   float dsum, derr;
-  two_sum(S, yh[12], dsum, derr);
+  two_sum(S, y[12], dsum, derr);
   out[0] = dsum + derr;
-  out[1] = yh[16];
-  out[2] = yh[17];
-  out[3] = yh[18];
+  out[1] = y[16];
+  out[2] = y[17];
+  out[3] = y[18];
+}
+
+SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6]) {
+  MixedRay R;
+  float y[kMixedState], x0[3];
+  mixed_observer(G, x0);
+  init_mixed(d, R, y);
+#pragma unroll 1
+  for (int step = 0; step < n_steps; ++step) step_mixed(R, F, G, x0, step, y, nullptr);
+  extract_mixed(R, n_steps, y, out);
 }
 
 // Ray direction of a RING pixel centre (FP64: cos/sin of the colatitude from
