@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--compare-batch", type=int, default=5, help="batch used for the FP64 / REF16 legs (-1: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--oracle-sample", type=int, default=24, help="pixels checked against the FP64 oracle")
+    ap.add_argument("--adjoint", default="256,128,128,12",
+                    help="adjoint leg: grid,nside,n_steps,ckpt_every ('' to skip)")
     return ap.parse_args()
 
 
@@ -199,6 +201,83 @@ def time_cpu(fn, target_s, make_sample, start=16):
         fn(pix)
         dt = time.perf_counter() - t0
     return len(pix), dt
+
+
+# ------------------------------------------------------------ adjoint leg
+
+def run_adjoint_leg(spec, seed, dev):
+    """Mixed forward vs mixed vjp (loss = sum of seeded N(0,1) pixel weights x
+    maps) at grid,nside,n_steps with checkpoints every ckpt_every steps; the
+    gradient is checked against the deterministic FP64 vjp (whole grid) and, on
+    a 64-pixel range, against the oracle's FP64 forward-mode tangent."""
+    import torch
+
+    import srt
+    import srt_fields
+    from oracle import oracle
+
+    n, nside, S, C = [int(x) for x in spec.split(",")]
+    npix = 12 * nside * nside
+    phi, b = srt_fields.gaussian_fields_torch(n, seed=seed + 101, device=dev)
+    w = torch.from_numpy(np.random.default_rng(seed).standard_normal((6, npix)).astype(np.float32)).to(dev)
+    out = torch.empty((6, npix), dtype=torch.float32, device=dev)
+    gphi = torch.zeros_like(phi)
+    gb = torch.zeros_like(b)
+    stream = torch.cuda.current_stream(dev)
+    res = {"workload": "%d^3, nside %d (%d rays), %d steps, checkpoints every %d steps" % (n, nside, npix, S, C)}
+    with srt.Fields(phi, b, stream=stream) as f:
+        fwd, adj = [], []
+        for i in range(4):
+            _, st = f.forward(nside, S, precision="mixed", out=out, stream=stream)
+            _, _, sa = f.vjp(nside, S, w, precision="mixed", dphi=gphi, db_xyz=gb, ckpt_every=C, stream=stream)
+            if i > 0:
+                fwd.append(st.trace_ms)
+                adj.append(sa.trace_ms)
+        res["forward_ms"] = float(np.median(fwd))
+        res["vjp_ms"] = float(np.median(adj))
+        res["vjp_over_forward"] = res["vjp_ms"] / res["forward_ms"]
+        res["vjp_ray_steps_per_s"] = npix * S / (res["vjp_ms"] * 1e-3)
+        # accuracy: mixed vjp vs deterministic FP64 vjp over the whole grid
+        g64 = torch.zeros_like(phi)
+        b64 = torch.zeros_like(b)
+        _, _, s64 = f.vjp(nside, S, w, precision="fp64", dphi=g64, db_xyz=b64, ckpt_every=C, deterministic=True,
+                          stream=stream)
+        torch.cuda.synchronize()
+        res["fp64_deterministic_vjp_ms"] = s64.trace_ms
+
+        def rel(a, r):
+            a, r = a.double(), r.double()
+            return float(torch.linalg.vector_norm(a - r) / torch.linalg.vector_norm(r))
+
+        res["mixed_vs_fp64_grad_rel_l2"] = {"phi": rel(gphi, g64), "B": rel(gb, b64)}
+        # dot-product test on a 64-pixel range against the oracle tangent
+        lo, cnt = 5 * nside * nside + nside, 64
+        wpart = w[:, lo:lo + cnt].contiguous()
+        gp = torch.zeros_like(phi)
+        bp = torch.zeros_like(b)
+        f.vjp(nside, S, wpart, pix_begin=lo, pix_count=cnt, precision="fp64", dphi=gp, db_xyz=bp, ckpt_every=C,
+              stream=stream)
+        gpm = torch.zeros_like(phi)
+        bpm = torch.zeros_like(b)
+        f.vjp(nside, S, wpart, pix_begin=lo, pix_count=cnt, precision="mixed", dphi=gpm, db_xyz=bpm, ckpt_every=C,
+              stream=stream)
+        torch.cuda.synchronize()
+    phi_np, b_np = phi.cpu().numpy(), b.cpu().numpy()
+    rng = np.random.default_rng(seed + 7)
+    dp = [rng.standard_normal(phi_np.shape).astype(np.float32) for _ in range(2)] + [None, None]
+    db = [None, None] + [rng.standard_normal(b_np.shape).astype(np.float32) for _ in range(2)]
+    _, dL = oracle.tangent(phi_np, b_np, nside, S, np.arange(lo, lo + cnt), wpart.cpu().numpy(), dp, db)
+    checks = []
+    for k in range(4):
+        for name, g_, b_ in (("fp64", gp, bp), ("mixed", gpm, bpm)):
+            got = (float(np.dot(g_.cpu().numpy().ravel().astype(np.float64), dp[k].ravel())) if dp[k] is not None
+                   else float(np.dot(b_.cpu().numpy().ravel().astype(np.float64), db[k].ravel())))
+            checks.append({"direction": k, "vjp": name, "rel_err": abs(got - dL[k]) / max(abs(dL[k]), 1e-300)})
+    res["tangent_check_64px"] = {"max_rel_err_fp64": max(c["rel_err"] for c in checks if c["vjp"] == "fp64"),
+                                 "max_rel_err_mixed": max(c["rel_err"] for c in checks if c["vjp"] == "mixed")}
+    del phi, b, gphi, gb, g64, b64, gp, bp, gpm, bpm, out, w
+    torch.cuda.empty_cache()
+    return res
 
 
 # --------------------------------------------------------------- our arm
@@ -332,6 +411,12 @@ def run_ours(args):
                                     "mixed_gpu_vs_oracle": map_errors(maps["mixed"][:, pix - b0], want)}
         result["compare"] = cmp
 
+    # ---- adjoint leg (rank 0)
+    if rank == 0 and args.adjoint:
+        fields.close()
+        fields = None
+        result["adjoint"] = run_adjoint_leg(args.adjoint, args.seed, dev)
+
     # ---- CPU baseline: FP64 oracle on a bounded sample (rank 0, N = 1 only)
     if rank == 0 and world == 1 and phi_np is not None and args.cpu_seconds > 0:
         from oracle import oracle
@@ -343,7 +428,8 @@ def run_ours(args):
         result["cpu_baseline"] = {"value": rays * S / dt, "unit": "ray-steps/s", "cores": cores, "kind": "port",
                                   "sample": "%d random pixels of the same workload x %d steps, FP64 oracle, "
                                             "%.1f s" % (rays, S, dt)}
-    fields.close()
+    if fields is not None:
+        fields.close()
     if rank == 0:
         print(json.dumps(result))
     if world > 1:

@@ -69,6 +69,9 @@ extern "C" {
                                 overwriting them */
 #define SRT_DETERMINISTIC 16u /* srt_vjp: order-independent (bitwise
                                  reproducible) FP64 gradient accumulation */
+#define SRT_FIELDS_NO_PAIRS 32u /* srt_fields_create: do not build the row-pair
+                                   copies of the fields (2x the field memory)
+                                   that the MIXED forward reads when present */
 
 #define SRT_NUM_MAPS 6
 
@@ -106,6 +109,9 @@ int srt_device_count(void);
  * (B_x, B_y, B_z of voxel v at b_xyz[3v+0..2]), the layout of the reference's
  * HDF5 vector read (snapshot-raytracer.cu:89-186). Host inputs are streamed
  * in slabs, so peak device memory is the laid-out fields plus one slab.
+ * Unless SRT_FIELDS_NO_PAIRS, and when device memory allows, each field is
+ * also stored as row pairs (f(i,j,k), f(i,j+1,k)) for the packed-FMA MIXED
+ * forward; without them MIXED reads the single copy.
  * Replaces snapshot-raytracer.cu:752-855 (cudaMalloc of the fields, the three
  * staged vector3_to_half passes and the phi copy). */
 int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t n1,

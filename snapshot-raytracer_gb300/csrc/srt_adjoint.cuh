@@ -203,6 +203,66 @@ SRT_HD int sym_idx(int i, int j) {
 template <typename T>
 SRT_HD T symv(const T* h, int i, int j) { return h[sym_idx(i, j)]; }
 
+// One B component's share of rhs_vjp: its cotangents (value, gradient,
+// Hessian) from the state-only intermediate cotangents, the fused pass, the
+// forward aggregates and its terms of the state cotangents.
+template <int C, typename T, typename Acc>
+SRT_HD void vjp_b_component(const StageView<T>& V, const FieldPtrs& F, const Geom& G, const T* fb, const T* ngBb, T e1b,
+                            T e2b, T nlapb, const T* Tb, const Acc& acc, T* xb, T* nb, T* ab, T* bb, T* ngB, T& e1ngB,
+                            T& e2ngB, T& nlap, T* Tm) {
+  const T* n = V.n;
+  const T* a = V.a;
+  const T* b = V.b;
+  const T nc = n[C], ac = a[C], bc = b[C];
+  T qb[10];
+  qb[0] = -fb[C];
+  for (int i = 0; i < 3; ++i)
+    qb[1 + i] = nc * ngBb[i] + T(0.5) * e1b * (ac * n[i] + nc * a[i]) + T(0.5) * e2b * (bc * n[i] + nc * b[i]);
+  // Hessian cotangent: n_c Tb + n_c nlapb I - sym(e_c Tb_c. (x) n)
+  for (int i = 0; i < 3; ++i)
+    for (int j = i; j < 3; ++j) {
+      T m = nc * symv(Tb, i, j) + ((i == j) ? nc * nlapb : T(0));
+      m -= T(0.5) * (symv(Tb, C, i) * n[j] + symv(Tb, C, j) * n[i]);
+      // unique components: off-diagonals hold both halves
+      qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
+    }
+  Tri<T> Q;
+  tricubic_vjp<T, Acc>(F.b[C], V.base[C], G.px, G.pxy, V.t[C][0], V.t[C][1], V.t[C][2], qb, Q, xb, acc);
+  // forward aggregates
+  for (int i = 0; i < 3; ++i) ngB[i] += Q.g[i] * nc;
+  const T gn = Q.g[0] * n[0] + Q.g[1] * n[1] + Q.g[2] * n[2];
+  const T ga = Q.g[0] * a[0] + Q.g[1] * a[1] + Q.g[2] * a[2];
+  const T gbb = Q.g[0] * b[0] + Q.g[1] * b[1] + Q.g[2] * b[2];
+  e1ngB += T(0.5) * (ac * gn + nc * ga);
+  e2ngB += T(0.5) * (bc * gn + nc * gbb);
+  T Hn[3];
+  for (int i = 0; i < 3; ++i) Hn[i] = symv(Q.h, i, 0) * n[0] + symv(Q.h, i, 1) * n[1] + symv(Q.h, i, 2) * n[2];
+  for (int i = 0; i < 3; ++i)
+    for (int j = i; j < 3; ++j) {
+      T d = Q.h[sym_idx(i, j)] * nc;
+      if (i == C) d -= T(0.5) * Hn[j];
+      if (j == C) d -= T(0.5) * Hn[i];
+      Tm[sym_idx(i, j)] += d;
+    }
+  const T trH = Q.h[0] + Q.h[3] + Q.h[5];
+  nlap += trH * nc;
+  // this component's share of the state cotangents
+  T HT = 0;  // H_c : Tb (full contraction)
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) HT += symv(Q.h, i, j) * symv(Tb, i, j);
+  nb[C] += Q.g[0] * ngBb[0] + Q.g[1] * ngBb[1] + Q.g[2] * ngBb[2] + trH * nlapb + HT + T(0.5) * e1b * ga +
+           T(0.5) * e2b * gbb;
+  for (int k = 0; k < 3; ++k) {
+    T tk = 0;
+    for (int j = 0; j < 3; ++j) tk += symv(Tb, C, j) * symv(Q.h, j, k);
+    nb[k] += T(0.5) * e1b * ac * Q.g[k] + T(0.5) * e2b * bc * Q.g[k] - tk;
+    ab[k] += T(0.5) * e1b * nc * Q.g[k];
+    bb[k] += T(0.5) * e2b * nc * Q.g[k];
+  }
+  ab[C] += T(0.5) * e1b * gn;
+  bb[C] += T(0.5) * e2b * gn;
+}
+
 // yb += J(u)^T fb for the stage described by V; tap cotangents go to acc[0..3]
 // (B_x, B_y, B_z, phi).
 template <typename T, typename Acc>
@@ -264,61 +324,13 @@ SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, co
   // aggregates of the forward
   T ngB[3] = {0, 0, 0}, e1ngB = 0, e2ngB = 0, nlap = 0, Tm[6] = {0, 0, 0, 0, 0, 0};
 
-  // ---- B components
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    const T nc = c == 0 ? n[0] : (c == 1 ? n[1] : n[2]);
-    const T ac = c == 0 ? a[0] : (c == 1 ? a[1] : a[2]);
-    const T bc = c == 0 ? b[0] : (c == 1 ? b[1] : b[2]);
-    T qb[10];
-    qb[0] = -fb[c];
-    for (int i = 0; i < 3; ++i)
-      qb[1 + i] = nc * ngBb[i] + T(0.5) * e1b * (ac * n[i] + nc * a[i]) + T(0.5) * e2b * (bc * n[i] + nc * b[i]);
-    // Hessian cotangent: n_c Tb + n_c nlapb I - sym(e_c Tb_c. (x) n)
-    for (int i = 0; i < 3; ++i)
-      for (int j = i; j < 3; ++j) {
-        T m = nc * symv(Tb, i, j) + ((i == j) ? nc * nlapb : T(0));
-        m -= T(0.5) * (symv(Tb, c, i) * n[j] + symv(Tb, c, j) * n[i]);
-        // unique components: off-diagonals hold both halves
-        qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
-      }
-    Tri<T> Q;
-    tricubic_vjp<T, Acc>(F.b[c], V.base[c], G.px, G.pxy, V.t[c][0], V.t[c][1], V.t[c][2], qb, Q, xb, acc[c]);
-    // forward aggregates
-    for (int i = 0; i < 3; ++i) ngB[i] += Q.g[i] * nc;
-    const T gn = Q.g[0] * n[0] + Q.g[1] * n[1] + Q.g[2] * n[2];
-    const T ga = Q.g[0] * a[0] + Q.g[1] * a[1] + Q.g[2] * a[2];
-    const T gbb = Q.g[0] * b[0] + Q.g[1] * b[1] + Q.g[2] * b[2];
-    e1ngB += T(0.5) * (ac * gn + nc * ga);
-    e2ngB += T(0.5) * (bc * gn + nc * gbb);
-    T Hn[3];
-    for (int i = 0; i < 3; ++i) Hn[i] = symv(Q.h, i, 0) * n[0] + symv(Q.h, i, 1) * n[1] + symv(Q.h, i, 2) * n[2];
-    for (int i = 0; i < 3; ++i)
-      for (int j = i; j < 3; ++j) {
-        T d = Q.h[sym_idx(i, j)] * nc;
-        if (i == c) d -= T(0.5) * Hn[j];
-        if (j == c) d -= T(0.5) * Hn[i];
-        Tm[sym_idx(i, j)] += d;
-      }
-    const T trH = Q.h[0] + Q.h[3] + Q.h[5];
-    nlap += trH * nc;
-    // this component's share of the state cotangents
-    T HT = 0;  // H_c : Tb (full contraction)
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) HT += symv(Q.h, i, j) * symv(Tb, i, j);
-    const T dnc = Q.g[0] * ngBb[0] + Q.g[1] * ngBb[1] + Q.g[2] * ngBb[2] + trH * nlapb + HT +
-                  T(0.5) * e1b * ga + T(0.5) * e2b * gbb;
-    nb[c] += dnc;
-    for (int k = 0; k < 3; ++k) {
-      T tk = 0;
-      for (int j = 0; j < 3; ++j) tk += symv(Tb, c, j) * symv(Q.h, j, k);
-      nb[k] += T(0.5) * e1b * ac * Q.g[k] + T(0.5) * e2b * bc * Q.g[k] - tk;
-      ab[k] += T(0.5) * e1b * nc * Q.g[k];
-      bb[k] += T(0.5) * e2b * nc * Q.g[k];
-    }
-    ab[c] += T(0.5) * e1b * gn;
-    bb[c] += T(0.5) * e2b * gn;
-  }
+  // ---- B components (compile-time component index: no local-memory arrays)
+  vjp_b_component<0, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[0], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
+                             Tm);
+  vjp_b_component<1, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[1], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
+                             Tm);
+  vjp_b_component<2, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[2], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
+                             Tm);
 
   // ---- phi
   Tri<T> P;

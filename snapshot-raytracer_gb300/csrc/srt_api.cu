@@ -57,6 +57,7 @@ Geom make_geom(const srt_fields* f) {
   }
   g.px = f->pn[0];
   g.pxy = f->pn[0] * f->pn[1];
+  g.pxy2 = f->pn[0] * (f->pn[1] - 1);
   return g;
 }
 
@@ -67,6 +68,7 @@ FieldPtrs make_ptrs(const srt_fields* f) {
     p.b[c] = f->b[c];
     p.bh[c] = f->bh[c];
   }
+  for (int c = 0; c < 4; ++c) p.pr[c] = f->pr[c];
   return p;
 }
 
@@ -159,6 +161,20 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
     if (!(flags & SRT_ASYNC) || slab) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
     if (slab) cudaFree(slab);
     slab = nullptr;
+    if (!(flags & SRT_FIELDS_NO_PAIRS)) {
+      // row-pair arrays for the packed MIXED path, when they fit with room to spare
+      const int64_t pair_bytes = 4 * f->pn[0] * (f->pn[1] - 1) * f->pn[2] * (int64_t)sizeof(float2);
+      size_t free_b = 0, total_b = 0;
+      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && pair_bytes + (int64_t(4) << 30) < (int64_t)free_b) {
+        const float* srcs[4] = {f->b[0], f->b[1], f->b[2], f->phi};
+        for (int c = 0; c < 4; ++c) {
+          SRT_CUDA_TRY(cudaMalloc(&f->pr[c], pair_bytes / 4), "cudaMalloc(row pairs)");
+          SRT_CUDA_TRY(launch_pair_build(srcs[c], f->pr[c], f->pn, s), "row pairs");
+        }
+        f->bytes += pair_bytes;
+        if (!(flags & SRT_ASYNC)) SRT_CUDA_TRY(cudaStreamSynchronize(s), "row pairs");
+      }
+    }
   }
   *out = f;
   return SRT_OK;
@@ -178,6 +194,7 @@ int srt_fields_destroy(srt_fields* f) {
     cudaFree(f->b[c]);
     cudaFree(f->bh[c]);
   }
+  for (int c = 0; c < 4; ++c) cudaFree(f->pr[c]);
   if (prev != f->device) cudaSetDevice(prev);
   delete f;
   return SRT_OK;
@@ -258,7 +275,8 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
       SRT_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
       SRT_CUDA_TRY(cudaEventRecord(e0, s), "cudaEventRecord");
     }
-    SRT_CUDA_TRY(launch_trace(precision, a, s, &kernels), "trace kernel launch");
+    const int kmode = (precision == SRT_PRECISION_MIXED && f->pr[0]) ? kMIXED_PAIR : precision;
+    SRT_CUDA_TRY(launch_trace(kmode, a, s, &kernels), "trace kernel launch");
     if (timed) SRT_CUDA_TRY(cudaEventRecord(e1, s), "cudaEventRecord");
     if (!dev_out) {
       for (int m = 0; m < 6; ++m)

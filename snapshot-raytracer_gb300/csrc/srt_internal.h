@@ -15,6 +15,7 @@ struct srt_fields {
   float* phi = nullptr;       // padded FP32 planes
   float* b[3] = {nullptr, nullptr, nullptr};
   __half* bh[3] = {nullptr, nullptr, nullptr};  // padded half(B * 2^27), made on first REF16 use
+  float2* pr[4] = {nullptr, nullptr, nullptr, nullptr};  // row-pair arrays B_x, B_y, B_z, phi (MIXED fast path)
   int64_t bytes = 0;
 };
 
@@ -42,6 +43,7 @@ FieldPtrs make_ptrs(const srt_fields* f);
 cudaError_t launch_pad_slab(const float* src, int comps, int comp, float* dst, const int64_t n[3],
                             const int64_t pn[3], int64_t k0, int64_t k1, cudaStream_t s);
 cudaError_t launch_quantize_half(const float* src, __half* dst, int64_t count, cudaStream_t s);
+cudaError_t launch_pair_build(const float* src, float2* dst, const int64_t pn[3], cudaStream_t s);
 
 // Trace kernel launch (mode = kFP64 / kMIXED / kREF16).
 cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* kernels);

@@ -65,6 +65,24 @@ cudaError_t launch_quantize_half(const float* src, __half* dst, int64_t count, c
   return cudaGetLastError();
 }
 
+// Row-pair array of a padded field: element (i, j, k), j < py - 1, holds
+// (f(i, j, k), f(i, j + 1, k)).
+__global__ void pair_build_kernel(const float* __restrict__ src, float2* __restrict__ dst, int64_t px, int64_t py,
+                                  int64_t pz) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t rows = py - 1;
+  if (q >= px * rows * pz) return;
+  const int64_t i = q % px, j = (q / px) % rows, k = q / (px * rows);
+  const int64_t s0 = i + px * (j + py * k);
+  dst[q] = make_float2(src[s0], src[s0 + px]);
+}
+
+cudaError_t launch_pair_build(const float* src, float2* dst, const int64_t pn[3], cudaStream_t s) {
+  const int64_t count = pn[0] * (pn[1] - 1) * pn[2];
+  pair_build_kernel<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(src, dst, pn[0], pn[1], pn[2]);
+  return cudaGetLastError();
+}
+
 // -------------------------------------------------------------------- trace
 
 // Resident blocks of 128 threads per SM the mixed kernel is compiled for
@@ -74,7 +92,8 @@ cudaError_t launch_quantize_half(const float* src, __half* dst, int64_t count, c
 #endif
 
 template <int MODE>
-__global__ void __launch_bounds__(128, MODE == kMIXED ? SRT_MIXED_MIN_BLOCKS : 1) trace_kernel(const TraceArgs A) {
+__global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ? SRT_MIXED_MIN_BLOCKS : 1)
+    trace_kernel(const TraceArgs A) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= A.launch_rays) return;
   // launch order: face-major, Morton (NESTED for power-of-two nside) in-face
@@ -87,10 +106,12 @@ __global__ void __launch_bounds__(128, MODE == kMIXED ? SRT_MIXED_MIN_BLOCKS : 1
   if (o < 0 || o >= A.pix_count) return;
   const RayDir d = ray_dir_pix(A.nside, ring);
   float out[6];
-  if (MODE == kMIXED)
-    trace_ray_mixed(A.F, A.G, d, A.n_steps, out);
+  if (MODE == kMIXED_PAIR)
+    trace_ray_mixed<true>(A.F, A.G, d, A.n_steps, out);
+  else if (MODE == kMIXED)
+    trace_ray_mixed<false>(A.F, A.G, d, A.n_steps, out);
   else
-    trace_ray_std<MODE>(A.F, A.G, d, A.n_steps, out);
+    trace_ray_std<MODE == kREF16 ? kREF16 : kFP64>(A.F, A.G, d, A.n_steps, out);
 #pragma unroll
   for (int m = 0; m < 6; ++m) A.maps[m][o] = out[m];
 }
@@ -103,6 +124,7 @@ cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* 
     case kFP64: trace_kernel<kFP64><<<(unsigned)blocks, threads, 0, s>>>(a); break;
     case kMIXED: trace_kernel<kMIXED><<<(unsigned)blocks, threads, 0, s>>>(a); break;
     case kREF16: trace_kernel<kREF16><<<(unsigned)blocks, threads, 0, s>>>(a); break;
+    case kMIXED_PAIR: trace_kernel<kMIXED_PAIR><<<(unsigned)blocks, threads, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   if (kernels) ++*kernels;

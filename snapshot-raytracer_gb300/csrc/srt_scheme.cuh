@@ -43,7 +43,7 @@
 
 namespace srt {
 
-enum { kFP64 = 0, kMIXED = 1, kREF16 = 2 };
+enum { kFP64 = 0, kMIXED = 1, kREF16 = 2, kMIXED_PAIR = 3 };
 
 #if defined(__CUDA_ARCH__)
 template <typename T>
@@ -58,6 +58,7 @@ SRT_HD T ldg(const T* p) { return *p; }
 struct Geom {
   int n[3];
   int64_t px, pxy;
+  int64_t pxy2;  // slice stride of the row-pair arrays (float2 units): px * (py - 1)
   float invn[3];
 };
 
@@ -65,6 +66,9 @@ struct FieldPtrs {
   const float* phi;     // padded FP32
   const float* b[3];    // padded FP32 B components
   const __half* bh[3];  // padded half(B * 2^27) (REF16 only)
+  // Row-pair arrays (MIXED fast path, optional): element (i, j, k), j < py - 1,
+  // holds (f(i, j, k), f(i, j + 1, k)) of the padded field; [0..2] B, [3] phi.
+  const float2* pr[4];
 };
 
 template <typename T>
@@ -155,6 +159,84 @@ SRT_HD void tri_scale(Tri<T>& r, T s) {
   for (int i = 0; i < 6; ++i) r.h[i] *= s;
 }
 
+// ------------------------------------------------ packed (FFMA2) tricubic
+
+#if defined(__CUDA_ARCH__)
+SRT_HD float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+SRT_HD float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+#else
+SRT_HD float2 ffma2(float2 a, float2 b, float2 c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
+SRT_HD float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+#endif
+SRT_HD float2 dup2(float v) { return make_float2(v, v); }
+
+// The same interpolation as `tricubic`, from the row-pair array: rows y and
+// y+1 of a slice arrive together in one 64-bit load per x tap, and every
+// pass runs on packed pairs (two FP32 FMAs per instruction): the x pass on
+// the two rows at once with duplicated x weights, the y pass with the weights
+// of rows (0, 1) and (2, 3), the z pass on even/odd partial sums that are
+// added at the end. base: the pair index of voxel (cx-1, cy-1, cz-1).
+SRT_HD void tricubic_pair(const float2* __restrict__ f, int64_t base, int64_t px, int64_t pxy2, const CRW<float>& X,
+                          const CRW<float>& Y, const CRW<float>& Z, Tri<float>& r) {
+  float2 xw[4], xg[4], xh[4];
+  for (int i = 0; i < 4; ++i) {
+    xw[i] = dup2(X.w[i]);
+    xg[i] = dup2(X.g[i]);
+    xh[i] = dup2(X.h[i]);
+  }
+  const float2 yw[2] = {make_float2(Y.w[0], Y.w[1]), make_float2(Y.w[2], Y.w[3])};
+  const float2 yg[2] = {make_float2(Y.g[0], Y.g[1]), make_float2(Y.g[2], Y.g[3])};
+  const float2 yh[2] = {make_float2(Y.h[0], Y.h[1]), make_float2(Y.h[2], Y.h[3])};
+  const float2 z0 = make_float2(0.f, 0.f);
+  float2 V = z0, G0 = z0, G1 = z0, G2 = z0, H00 = z0, H01 = z0, H02 = z0, H11 = z0, H12 = z0, H22 = z0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    float2 A = z0, AY = z0, AYY = z0, AX = z0, AXY = z0, AXX = z0;
+#pragma unroll
+    for (int pr = 0; pr < 2; ++pr) {
+      const float2* row = f + base + c * pxy2 + 2 * pr * px;
+      const float2 t0 = ldg(row + 0), t1 = ldg(row + 1), t2 = ldg(row + 2), t3 = ldg(row + 3);
+      float2 RV = fmul2(xw[0], t0), RX = fmul2(xg[0], t0), RXX = fmul2(xh[0], t0);
+      RV = ffma2(xw[1], t1, RV);
+      RX = ffma2(xg[1], t1, RX);
+      RXX = ffma2(xh[1], t1, RXX);
+      RV = ffma2(xw[2], t2, RV);
+      RX = ffma2(xg[2], t2, RX);
+      RXX = ffma2(xh[2], t2, RXX);
+      RV = ffma2(xw[3], t3, RV);
+      RX = ffma2(xg[3], t3, RX);
+      RXX = ffma2(xh[3], t3, RXX);
+      A = ffma2(yw[pr], RV, A);
+      AY = ffma2(yg[pr], RV, AY);
+      AYY = ffma2(yh[pr], RV, AYY);
+      AX = ffma2(yw[pr], RX, AX);
+      AXY = ffma2(yg[pr], RX, AXY);
+      AXX = ffma2(yw[pr], RXX, AXX);
+    }
+    const float2 zw = dup2(Z.w[c]), zg = dup2(Z.g[c]), zh = dup2(Z.h[c]);
+    V = ffma2(zw, A, V);
+    G0 = ffma2(zw, AX, G0);
+    G1 = ffma2(zw, AY, G1);
+    G2 = ffma2(zg, A, G2);
+    H00 = ffma2(zw, AXX, H00);
+    H01 = ffma2(zw, AXY, H01);
+    H02 = ffma2(zg, AX, H02);
+    H11 = ffma2(zw, AYY, H11);
+    H12 = ffma2(zg, AY, H12);
+    H22 = ffma2(zh, A, H22);
+  }
+  r.v = V.x + V.y;
+  r.g[0] = G0.x + G0.y;
+  r.g[1] = G1.x + G1.y;
+  r.g[2] = G2.x + G2.y;
+  r.h[0] = H00.x + H00.y;
+  r.h[1] = H01.x + H01.y;
+  r.h[2] = H02.x + H02.y;
+  r.h[3] = H11.x + H11.y;
+  r.h[4] = H12.x + H12.y;
+  r.h[5] = H22.x + H22.y;
+}
+
 // ------------------------------------------------------------ cell lookup
 
 SRT_HD int wrap64(int64_t c, int n) {
@@ -180,6 +262,11 @@ SRT_HD int wrap32(int c, int n, float invn) {
 
 SRT_HD int64_t cell_base(const Geom& G, int cx, int cy, int cz) {
   return (int64_t)cx + G.px * (int64_t)cy + G.pxy * (int64_t)cz;
+}
+
+// The same voxel's index in a row-pair array.
+SRT_HD int64_t cell_base_pair(const Geom& G, int cx, int cy, int cz) {
+  return (int64_t)cx + G.px * (int64_t)cy + G.pxy2 * (int64_t)cz;
 }
 
 // FP64 / REF16 interpolation of one field at a double-precision position.
@@ -454,15 +541,20 @@ struct BAcc {
 // B component C interpolated at the position staggered by -1/2 along axis C,
 // folded into the accumulators. C is a compile-time constant so n[C], a[C]
 // and b[C] stay in registers.
-template <int C>
-SRT_HD void add_b_component(const float* __restrict__ field, const Geom& G, const int* cc, const int* cs,
+template <int C, bool PAIR>
+SRT_HD void add_b_component(const FieldPtrs& F, const Geom& G, const int* cc, const int* cs,
                             const float* ts, const CRW<float>& Cx, const CRW<float>& Cy, const CRW<float>& Cz,
                             const float* n, const float* a, const float* b, BAcc& A) {
   CRW<float> S;
   cr_weights(ts[C], S);
-  const int64_t base = cell_base(G, C == 0 ? cs[0] : cc[0], C == 1 ? cs[1] : cc[1], C == 2 ? cs[2] : cc[2]);
+  const int cx = C == 0 ? cs[0] : cc[0], cy = C == 1 ? cs[1] : cc[1], cz = C == 2 ? cs[2] : cc[2];
   Tri<float> r;
-  tricubic<float, float>(field, base, G.px, G.pxy, C == 0 ? S : Cx, C == 1 ? S : Cy, C == 2 ? S : Cz, r);
+  if (PAIR)
+    tricubic_pair(F.pr[C], cell_base_pair(G, cx, cy, cz), G.px, G.pxy2, C == 0 ? S : Cx, C == 1 ? S : Cy,
+                  C == 2 ? S : Cz, r);
+  else
+    tricubic<float, float>(F.b[C], cell_base(G, cx, cy, cz), G.px, G.pxy, C == 0 ? S : Cx, C == 1 ? S : Cy,
+                           C == 2 ? S : Cz, r);
   A.val[C] = r.v;
   for (int i = 0; i < 3; ++i) A.ngB[i] += r.g[i] * n[C];
   const float gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
@@ -485,6 +577,7 @@ SRT_HD void add_b_component(const float* __restrict__ field, const Geom& G, cons
 // Perturbation right-hand side g = f(y0(s) + d) - f(y0(s)) (FP32). `s` is the
 // affine parameter of the stage (step + 0, 1/2 or 1), d the stage state
 // (delta components in the layout of rhs_std), x0 the observer.
+template <bool PAIR>
 SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtrs& F, const Geom& G,
                       const float* x0, float* g) {
   float Dn[3], Da[3], Db[3];
@@ -517,11 +610,14 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   A.ngB[0] = A.ngB[1] = A.ngB[2] = 0.f;
   A.e1ngB = A.e2ngB = A.nlap = 0.f;
   for (int i = 0; i < 6; ++i) A.T[i] = 0.f;
-  add_b_component<0>(F.b[0], G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
-  add_b_component<1>(F.b[1], G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
-  add_b_component<2>(F.b[2], G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
+  add_b_component<0, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
+  add_b_component<1, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
+  add_b_component<2, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
   Tri<float> p;
-  tricubic<float, float>(F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy, Cx, Cy, Cz, p);
+  if (PAIR)
+    tricubic_pair(F.pr[3], cell_base_pair(G, cc[0], cc[1], cc[2]), G.px, G.pxy2, Cx, Cy, Cz, p);
+  else
+    tricubic<float, float>(F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy, Cx, Cy, Cz, p);
 
   const float dA = s + d[12];
   const float dAp = d[13] - 1.f;
@@ -573,10 +669,13 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   }
 }
 
-// Number of leading state components accumulated with a compensation term:
-// the ray position, whose increments are ~1e-4 of its size after a few hundred
-// steps and whose error becomes the deflection error.
-constexpr int kCompensated = 3;
+// Number of leading state components accumulated with a compensation term
+// (all of them). The ray position and direction matter most: the position's
+// increments are ~1e-4 of its size after a few hundred steps, and any error in
+// either moves the trajectory, which changes where the ray crosses cell faces
+// (Catmull-Rom's Hessian jumps there); rounding the direction alone doubles the
+// deflection error and raises the rate of such crossings.
+constexpr int kCompensated = 19;
 // Floats of one stored MIXED state: the 19 components and the compensations.
 constexpr int kMixedState = 19 + kCompensated;
 
@@ -618,6 +717,7 @@ SRT_HD void mixed_stage(const float* y, const float* k, float c, float* ys) {
 
 // One RK4 step from affine parameter `step`; when ks is given, the stage
 // derivatives k1, k2, k3 are stored there (3 x 19).
+template <bool PAIR = false>
 SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, const float* x0, int step, float* y,
                        float* ks) {
   float k[19], acc[19], ys[19];
@@ -627,7 +727,7 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
   for (int st = 0; st < 4; ++st) {
     const float c = (st == 0) ? 0.f : ((st == 3) ? 1.f : 0.5f);
     mixed_stage(y, k, c, ys);
-    rhs_mixed(ys, s0 + c, R, F, G, x0, k);
+    rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k);
     if (ks && st < 3)
       for (int j = 0; j < 19; ++j) ks[19 * st + j] = k[j];
     for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
@@ -663,13 +763,14 @@ SRT_HD void extract_mixed(const MixedRay& R, int n_steps, const float* y, float 
   out[3] = y[18];
 }
 
+template <bool PAIR = false>
 SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6]) {
   MixedRay R;
   float y[kMixedState], x0[3];
   mixed_observer(G, x0);
   init_mixed(d, R, y);
 #pragma unroll 1
-  for (int step = 0; step < n_steps; ++step) step_mixed(R, F, G, x0, step, y, nullptr);
+  for (int step = 0; step < n_steps; ++step) step_mixed<PAIR>(R, F, G, x0, step, y, nullptr);
   extract_mixed(R, n_steps, y, out);
 }
 

@@ -25,6 +25,7 @@ SRT_OUTPUT_DEVICE = 2
 SRT_ASYNC = 4
 SRT_ACCUMULATE = 8
 SRT_DETERMINISTIC = 16
+SRT_FIELDS_NO_PAIRS = 32
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
           -5: "format error", -6: "no CUDA device", -7: "unsupported"}
@@ -152,7 +153,7 @@ class Fields:
     """Laid-out phi and B on the GPU (srt_fields_create). phi: (n2, n1, n0)
     float32; b_xyz: (n2, n1, n0, 3) float32; numpy (host) or CUDA tensors."""
 
-    def __init__(self, phi, b_xyz, stream=None, async_=False):
+    def __init__(self, phi, b_xyz, stream=None, async_=False, pairs=True):
         shape = tuple(phi.shape)
         if len(shape) != 3 or tuple(b_xyz.shape) != shape + (3,):
             raise ValueError("phi must be (n2, n1, n0) and b_xyz (n2, n1, n0, 3); got %r and %r"
@@ -165,7 +166,8 @@ class Fields:
         if dev_phi != dev_b:
             raise ValueError("phi and b_xyz must both be on the host or both on the device")
         self.n = (shape[2], shape[1], shape[0])
-        flags = (SRT_INPUT_DEVICE if dev_phi else 0) | (SRT_ASYNC if async_ else 0)
+        flags = (SRT_INPUT_DEVICE if dev_phi else 0) | (SRT_ASYNC if async_ else 0) | \
+            (0 if pairs else SRT_FIELDS_NO_PAIRS)
         h = _P()
         _check(lib().srt_fields_create(p_phi, p_b, self.n[0], self.n[1], self.n[2], flags, _stream_ptr(stream),
                                        ctypes.byref(h)))

@@ -52,12 +52,13 @@ def test_fp64_matches_oracle(golden, srt, orc, case):
     _assert_close(got, want, "fp64", case)
 
 
+@pytest.mark.parametrize("pairs", [True, False], ids=["pair-layout", "single-layout"])
 @pytest.mark.parametrize("case", CASES)
-def test_mixed_matches_oracle(golden, srt, orc, case):
+def test_mixed_matches_oracle(golden, srt, orc, case, pairs):
     meta, _ = golden
     phi, b = golden_fields(meta, case)
     nside, steps, begin, count = _range(meta, case)
-    with srt.Fields(phi, b) as f:
+    with srt.Fields(phi, b, pairs=pairs) as f:
         got, _ = f.forward(nside, steps, begin, count, "mixed")
     want = orc.trace(phi, b, nside, steps, begin, count, mode="fp64")
     _assert_close(got, want, "mixed", case)
@@ -138,11 +139,11 @@ def test_deterministic(srt):
     assert np.array_equal(a.view(np.uint32), c.view(np.uint32))
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed"])
-def test_gaussian_fields_vs_oracle(srt, orc, mode):
+@pytest.mark.parametrize("mode,pairs", [("fp64", True), ("mixed", True), ("mixed", False)])
+def test_gaussian_fields_vs_oracle(srt, orc, mode, pairs):
     phi, b = srt_fields.gaussian_fields_np(64, seed=7)
     nside, steps = 8, 48
-    with srt.Fields(phi, b) as f:
+    with srt.Fields(phi, b, pairs=pairs) as f:
         got, _ = f.forward(nside, steps, precision=mode)
     want = orc.trace(phi, b, nside, steps, mode="fp64")
     _assert_close(got, want, mode, "gaussian64")
@@ -171,7 +172,10 @@ def test_larger_grid_mixed_vs_fp64_and_oracle_sample(srt, orc):
     with srt.Fields(phi, b) as f:
         m64, _ = f.forward(nside, steps, precision="fp64")
         mmx, _ = f.forward(nside, steps, precision="mixed")
+    with srt.Fields(phi, b, pairs=False) as f:
+        mmx1, _ = f.forward(nside, steps, precision="mixed")
     _assert_close(mmx, m64, "mixed", "mixed vs fp64 @256^3")
+    _assert_close(mmx1, m64, "mixed", "mixed (single layout) vs fp64 @256^3")
     pix = np.random.default_rng(0).choice(12 * nside * nside, 96, replace=False)
     want = orc.trace_pixels(phi, b, nside, steps, pix, mode="fp64")
     _assert_close(m64[:, pix], want, "fp64", "fp64 sample @256^3")
