@@ -21,7 +21,9 @@ Also reported on the same line:
                same workload on all host cores.
 --impl reference times the reference's own CPU arithmetic for the path on the
 host cores (oracle/_ref where it was built from the reference sources, else
-the oracle's REF16 port) on bounded samples of the same workload.
+the oracle's REF16 port) on bounded samples of the same workload, and adds
+the reference's own GPU build (its raytracing_kernel, compiled unmodified)
+timed on one batch of the workload on this GPU as "gpu_build".
 """
 import argparse
 import json
@@ -60,6 +62,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-ref-gpu", dest="ref_gpu", action="store_false",
+                    help="reference arm: skip the reference's own GPU build")
     ap.add_argument("--n", type=int, default=1024, help="grid side")
     ap.add_argument("--nside", type=int, default=1024)
     ap.add_argument("--n-steps", type=int, default=512)
@@ -227,15 +231,20 @@ def run_adjoint_leg(spec, seed, dev):
     res = {"workload": "%d^3, nside %d (%d rays), %d steps, checkpoints every %d steps" % (n, nside, npix, S, C)}
     with srt.Fields(phi, b, stream=stream) as f:
         fwd, adj = [], []
+        fwd_nr = []
         for i in range(4):
             _, st = f.forward(nside, S, precision="mixed", out=out, stream=stream)
+            _, st2 = f.forward(nside, S, precision="mixed", out=out, stream=stream, refine=False)
             _, _, sa = f.vjp(nside, S, w, precision="mixed", dphi=gphi, db_xyz=gb, ckpt_every=C, stream=stream)
             if i > 0:
                 fwd.append(st.trace_ms)
+                fwd_nr.append(st2.trace_ms)
                 adj.append(sa.trace_ms)
         res["forward_ms"] = float(np.median(fwd))
+        res["forward_fp32_only_ms"] = float(np.median(fwd_nr))
         res["vjp_ms"] = float(np.median(adj))
         res["vjp_over_forward"] = res["vjp_ms"] / res["forward_ms"]
+        res["vjp_over_fp32_forward"] = res["vjp_ms"] / res["forward_fp32_only_ms"]
         res["vjp_ray_steps_per_s"] = npix * S / (res["vjp_ms"] * 1e-3)
         # accuracy: mixed vjp vs deterministic FP64 vjp over the whole grid
         g64 = torch.zeros_like(phi)
@@ -312,7 +321,7 @@ def run_ours(args):
         fields.forward(nside, S, precision=args.precision, out=out, stream=stream)
     torch.cuda.synchronize()
 
-    trace_ms, kernels = [], 0
+    trace_ms, kernels, refined = [], 0, []
     with ClockSampler(local) as clocks:
         barrier(world)
         torch.cuda.synchronize()
@@ -322,6 +331,7 @@ def run_ours(args):
             _, st = fields.forward(nside, S, precision=args.precision, out=out, stream=stream)
             trace_ms.append(st.trace_ms)
             kernels += st.kernels
+            refined.append(st.refined_rays)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier(world)
@@ -337,7 +347,8 @@ def run_ours(args):
               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
               "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else
               ("f64" if args.precision == "fp64" else "f32/f16"), "data": "synthetic", "config": cfg,
-              "gpu_launches": kernels}
+              "gpu_launches": kernels,
+              "refined_rays_per_step": int(np.max(refined)) if refined else 0}
     traffic = None
     prof = os.path.join(ROOT, "profiles", "trace_traffic.json")
     if os.path.isfile(prof):
@@ -394,7 +405,8 @@ def run_ours(args):
             fields.forward(nside, S, b0, cnt, precision=mode, out=bout, stream=stream)  # warm (REF16 builds its planes)
             _, st = fields.forward(nside, S, b0, cnt, precision=mode, out=bout, stream=stream)
             torch.cuda.synchronize()
-            legs[mode] = {"ray_steps_per_s": cnt * S / (st.trace_ms * 1e-3), "kernel_ms": st.trace_ms}
+            legs[mode] = {"ray_steps_per_s": cnt * S / (st.trace_ms * 1e-3), "kernel_ms": st.trace_ms,
+                          "refined_rays": st.refined_rays}
             maps[mode] = bout.cpu().numpy()
         cmp = {"batch": args.compare_batch, "rays": cnt, "legs": legs,
                "mixed_over_fp64": legs["mixed"]["ray_steps_per_s"] / legs["fp64"]["ray_steps_per_s"],
@@ -454,20 +466,20 @@ def run_reference(args):
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     phi_t, b_t = srt_fields.gaussian_fields_torch(n, seed=args.seed, device=dev)
     phi_np, b_np = phi_t.cpu().numpy(), b_t.cpu().numpy()
+    gpu_build = None
+    if dev == "cuda" and args.ref_gpu:
+        gpu_build = run_reference_gpu_build(oracle, phi_t, b_t, nside, S)
     del phi_t, b_t
     use_ref = oracle.ref_available()
     cores = oracle.max_threads()
-    if use_ref:
-        def run(pix):
-            # the reference's own host code traces contiguous RING ranges
-            oracle.ref_trace(phi_np, b_np, nside, S, int(pix[0]), len(pix), threads=cores)
-        make = lambda k: np.arange(k) + 5 * nside * nside  # noqa: E731
-        kind = "reference"
-    else:
-        def run(pix):
-            oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="ref16", threads=cores)
-        make = lambda k: sample_pixels(nside, k, seed=3)  # noqa: E731
-        kind = "port"
+    # the fields are staged once (FP16 B planes), outside the timed region, as
+    # the GPU arm's fields are resident before its timed region
+    ofields = oracle.Fields(phi_np, b_np, mode="ref16", reference=use_ref)
+
+    def run(pix):
+        ofields.trace_pixels(nside, S, pix, threads=cores)
+    make = lambda k: sample_pixels(nside, k, seed=3)  # noqa: E731
+    kind = "reference" if use_ref else "port"
     per_step_s = max(2.0, min(20.0, 60.0 / max(args.steps + args.warmup, 1)))
     rays, dt = time_cpu(run, per_step_s, make)
     pix = make(rays)
@@ -477,6 +489,7 @@ def run_reference(args):
     for _ in range(args.steps):
         run(pix)
     dt = (time.perf_counter() - t0) / args.steps
+    ofields.close()
     value = rays * S / dt
     sample = ("%d pixels x %d steps of the %d^3 / nside %d workload per step, %s" %
               (rays, S, n, nside, "reference host code (oracle/_ref)" if use_ref else
@@ -489,7 +502,27 @@ def run_reference(args):
            "cpu_baseline": {"value": value, "unit": "ray-steps/s", "cores": cores, "kind": kind, "sample": sample},
            "e2e": {"value": value, "unit": "ray-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "gpu_launches": 0}
+    if gpu_build is not None:
+        res["gpu_build"] = gpu_build
     print(json.dumps(res))
+
+
+def run_reference_gpu_build(oracle, phi_t, b_t, nside, S):
+    """The reference's own GPU build (raytracing_kernel compiled unmodified from
+    its source, launched as its main() launches it) on one batch of the same
+    workload on this GPU: kernel time by CUDA events, as a second reference
+    figure beside the CPU line."""
+    if not oracle.ref_gpu_available():
+        return {"unavailable": "reference cubin not built (needs the reference sources at build time)"}
+    begin, count = 5 * nside * nside, nside * nside
+    try:
+        _, ms = oracle.ref_gpu_trace(phi_t, b_t, nside, S, begin, count, reps=2)
+    except RuntimeError as e:
+        return {"unavailable": str(e)}
+    t = min(ms)
+    return {"value": count * S / (t * 1e-3), "unit": "ray-steps/s", "kernel_ms": t, "rays": count,
+            "sample": "batch 5 (RING pixels [5 nside^2, 6 nside^2)) x %d steps; min of 2 launches" % S,
+            "build": "nvcc -O3 --use_fast_math, sm_103a, reference source unmodified"}
 
 
 def main():

@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SRT_ABI_VERSION 1
+#define SRT_ABI_VERSION 2
 
 /* status codes */
 #define SRT_OK 0
@@ -72,6 +72,9 @@ extern "C" {
 #define SRT_FIELDS_NO_PAIRS 32u /* srt_fields_create: do not build the row-pair
                                    copies of the fields (2x the field memory)
                                    that the MIXED forward reads when present */
+#define SRT_MIXED_NO_REFINE 64u /* srt_forward, MIXED: keep the FP32 result of
+                                   rays that passed within 1e-7 cell of a cell
+                                   face instead of re-tracing them in FP64 */
 
 #define SRT_NUM_MAPS 6
 
@@ -85,6 +88,7 @@ typedef struct srt_stats {
   int64_t kernels;     /* kernels this call launched */
   int64_t h2d_bytes;   /* bytes copied host -> device by this call */
   int64_t d2h_bytes;   /* bytes copied device -> host by this call */
+  int64_t refined_rays; /* MIXED: rays re-traced in FP64 (synchronous calls) */
 } srt_stats;
 
 /* ---------------------------------------------------------------- library */
@@ -132,7 +136,12 @@ int64_t srt_fields_bytes(const srt_fields* fields);
  * pix_count floats, on the host unless SRT_OUTPUT_DEVICE).
  * Rays are set up from the pixel centres and the observer at the box centre on
  * the device and launched in NESTED order for locality; results are stored at
- * their RING index. The CLI's batch b is pix_begin = b*nside^2,
+ * their RING index. MIXED traces in FP32 and re-traces in FP64 the few rays
+ * (~0.15% at 512 steps) whose stage positions pass a cell face closer than
+ * the FP32 trajectory's error bound, 4e-7 (max|dx| + s max|dn|) + 1e-10 grid
+ * units, where the FP32 and FP64 trajectories could pick different cells (the
+ * Catmull-Rom Hessian jumps across faces); those rays then equal the FP64
+ * result bit for bit (SRT_MIXED_NO_REFINE skips this). The CLI's batch b is pix_begin = b*nside^2,
  * pix_count = nside^2 (snapshot-raytracer.cu:708-717); all pixels is
  * pix_begin = 0, pix_count = 12*nside^2.
  * Replaces snapshot-raytracer.cu:857-913 (pix2ang loop, theta/phi upload,

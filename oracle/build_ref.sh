@@ -13,3 +13,7 @@ mkdir -p "$HERE/_ref"
 nvcc -O3 --use_fast_math -std=c++17 -shared -Xcompiler -fopenmp,-fPIC,-ffp-contract=off \
   -gencode arch=compute_103a,code=sm_103a -w \
   -I"$HERE/stubs" -I"$REF" "$HERE/ref_harness.cu" -o "$HERE/_ref/libsrt_ref.so"
+# The reference's own device code as a cubin (vector3_to_half, raytracing_kernel),
+# launched by oracle/ref_gpu.cu to time the reference's GPU build on the same GPU.
+nvcc -cubin -O3 --use_fast_math -std=c++17 -gencode arch=compute_103a,code=sm_103a -w \
+  -I"$HERE/stubs" -I"$REF" "$HERE/ref_gpu_unit.cu" -o "$HERE/_ref/ref_kernel.cubin"

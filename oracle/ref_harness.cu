@@ -18,17 +18,41 @@
 
 #include <cstring>
 
-extern "C" int srtref_trace_angles(const float* phi, const float* b_xyz, int n0, int n1, int n2,
-                                   const double* theta, const double* phiang, int64_t nrays,
-                                   int n_steps, float* maps, int nthreads) {
+namespace {
+// The reference's device-side inputs, staged once: phi (the caller's array,
+// which must outlive the handle), B quantised as vector3_to_half does.
+struct RefFields {
+  const float* phi;
+  std::vector<__half> h1, h2, h3;
+  int dims[3];
+};
+}  // namespace
+
+extern "C" void* srtref_fields_new(const float* phi, const float* b_xyz, int n0, int n1, int n2) {
+  RefFields* f = new RefFields;
   const int64_t nv = (int64_t)n0 * n1 * n2;
-  std::vector<__half> h1(nv), h2(nv), h3(nv);
+  f->phi = phi;
+  f->h1.resize(nv);
+  f->h2.resize(nv);
+  f->h3.resize(nv);
+#pragma omp parallel for schedule(static)
   for (int64_t v = 0; v < nv; ++v) {
-    h1[v] = __float2half(b_xyz[3 * v + 0] * 134217728.0f);
-    h2[v] = __float2half(b_xyz[3 * v + 1] * 134217728.0f);
-    h3[v] = __float2half(b_xyz[3 * v + 2] * 134217728.0f);
+    f->h1[v] = __float2half(b_xyz[3 * v + 0] * 134217728.0f);
+    f->h2[v] = __float2half(b_xyz[3 * v + 1] * 134217728.0f);
+    f->h3[v] = __float2half(b_xyz[3 * v + 2] * 134217728.0f);
   }
-  const int dims[3] = {n0, n1, n2};
+  f->dims[0] = n0;
+  f->dims[1] = n1;
+  f->dims[2] = n2;
+  return f;
+}
+
+extern "C" void srtref_fields_delete(void* h) { delete (RefFields*)h; }
+
+extern "C" int srtref_trace_angles_h(void* h, const double* theta, const double* phiang, int64_t nrays, int n_steps,
+                                     float* maps, int nthreads) {
+  const RefFields* f = (const RefFields*)h;
+  const int* dims = f->dims;
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t i = 0; i < nrays; ++i) {
@@ -38,7 +62,7 @@ extern "C" int srtref_trace_angles(const float* phi, const float* b_xyz, int n0,
                     -std::sin(th) * std::sin(ph), -std::cos(th), std::cos(th) * std::cos(ph),
                     std::cos(th) * std::sin(ph), -std::sin(th), std::sin(ph), -std::cos(ph),
                     0.0, 0.0, -1.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    raytracing(phi, h1.data(), h2.data(), h3.data(), dims, y, n_steps);
+    raytracing(f->phi, f->h1.data(), f->h2.data(), f->h3.data(), dims, y, n_steps);
     y[0] -= static_cast<double>(dims[0]) * 0.5;
     y[1] -= static_cast<double>(dims[1]) * 0.5;
     y[2] -= static_cast<double>(dims[2]) * 0.5;
@@ -55,6 +79,15 @@ extern "C" int srtref_trace_angles(const float* phi, const float* b_xyz, int n0,
     maps[5 * nrays + i] = static_cast<float>(y[0] * std::sin(ph) - y[1] * std::cos(ph));
   }
   return 0;
+}
+
+extern "C" int srtref_trace_angles(const float* phi, const float* b_xyz, int n0, int n1, int n2,
+                                   const double* theta, const double* phiang, int64_t nrays,
+                                   int n_steps, float* maps, int nthreads) {
+  void* h = srtref_fields_new(phi, b_xyz, n0, n1, n2);
+  const int rc = srtref_trace_angles_h(h, theta, phiang, nrays, n_steps, maps, nthreads);
+  srtref_fields_delete(h);
+  return rc;
 }
 
 // The reference's own tricubic_interpolation (snapshot-raytracer.cu:215-312)

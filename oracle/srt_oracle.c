@@ -168,6 +168,11 @@ void srto_pix2ang_ring(int64_t nside, int64_t pix, double* theta, double* phi) {
   *theta = atan2(s, z);
 }
 
+/* theta, phi of RING pixels [begin, begin + count). */
+void srto_pix2ang_ring_range(int64_t nside, int64_t begin, int64_t count, double* theta, double* phi) {
+  for (int64_t i = 0; i < count; ++i) srto_pix2ang_ring(nside, begin + i, &theta[i], &phi[i]);
+}
+
 /* ------------------------------------------------------------ tracing */
 
 /* Initial state (snapshot-raytracer.cu:560) and extraction (:566-582) around
@@ -241,26 +246,48 @@ static void or_fields_free(or_fields* F) {
   for (int c = 0; c < 3; ++c) free(F->bh[c]);
 }
 
-/* Trace the RING pixels listed in `pix` (count entries) and write
- * maps[m * count + i] for map m of pixel pix[i]. Returns 0, or a negative
- * code on bad arguments / allocation failure. */
-int srto_trace_pixels(const float* phi, const float* b_xyz, int64_t n0, int64_t n1, int64_t n2,
-                      int64_t nside, const int64_t* pix, int64_t count, int n_steps, int mode,
-                      float* maps, int nthreads) {
-  if (n0 < 1 || n1 < 1 || n2 < 1 || nside < 1 || n_steps < 1 || count < 0) return -1;
-  if (mode != OR_MODE_FP64 && mode != OR_MODE_REF16) return -1;
-  const int64_t nv = n0 * n1 * n2, npix = 12 * nside * nside;
+/* Laid-out fields kept between calls (the planes and, for REF16, the FP16 B
+ * planes are built once; phi is read from the caller's array, which must
+ * outlive the handle). */
+typedef struct {
+  or_fields F;
+  float* planes;
+  int mode;
+} srto_handle;
+
+void* srto_fields_new(const float* phi, const float* b_xyz, int64_t n0, int64_t n1, int64_t n2, int mode) {
+  if (n0 < 1 || n1 < 1 || n2 < 1) return NULL;
+  if (mode != OR_MODE_FP64 && mode != OR_MODE_REF16) return NULL;
+  srto_handle* h = (srto_handle*)calloc(1, sizeof(srto_handle));
+  if (!h) return NULL;
+  h->mode = mode;
+  h->planes = (float*)malloc((size_t)(3 * n0 * n1 * n2) * sizeof(float));
+  if (!h->planes || or_fields_init(&h->F, phi, b_xyz, h->planes, n0, n1, n2, mode) != 0) {
+    or_fields_free(&h->F);
+    free(h->planes);
+    free(h);
+    return NULL;
+  }
+  return h;
+}
+
+void srto_fields_delete(void* hv) {
+  srto_handle* h = (srto_handle*)hv;
+  if (!h) return;
+  or_fields_free(&h->F);
+  free(h->planes);
+  free(h);
+}
+
+/* Trace the RING pixels listed in `pix` (count entries) through the fields of
+ * handle h and write maps[m * count + i] for map m of pixel pix[i]. */
+int srto_trace_pixels_h(void* hv, int64_t nside, const int64_t* pix, int64_t count, int n_steps, float* maps,
+                        int nthreads) {
+  srto_handle* h = (srto_handle*)hv;
+  if (!h || nside < 1 || n_steps < 1 || count < 0) return -1;
+  const int64_t npix = 12 * nside * nside;
   for (int64_t i = 0; i < count; ++i)
     if (pix[i] < 0 || pix[i] >= npix) return -1;
-  float* planes = (float*)malloc((size_t)(3 * nv) * sizeof(float));
-  if (!planes) return -3;
-  or_fields F;
-  memset(&F, 0, sizeof(F));
-  if (or_fields_init(&F, phi, b_xyz, planes, n0, n1, n2, mode) != 0) {
-    or_fields_free(&F);
-    free(planes);
-    return -3;
-  }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 1)
@@ -269,12 +296,28 @@ int srto_trace_pixels(const float* phi, const float* b_xyz, int64_t n0, int64_t 
     double th, ph;
     float out[6];
     srto_pix2ang_ring(nside, pix[i], &th, &ph);
-    or_trace_ray(&F, mode, th, ph, n_steps, out);
+    or_trace_ray(&h->F, h->mode, th, ph, n_steps, out);
     for (int m = 0; m < 6; ++m) maps[m * count + i] = out[m];
   }
-  or_fields_free(&F);
-  free(planes);
   return 0;
+}
+
+/* Trace the RING pixels listed in `pix` (count entries) and write
+ * maps[m * count + i] for map m of pixel pix[i]. Returns 0, or a negative
+ * code on bad arguments / allocation failure. */
+int srto_trace_pixels(const float* phi, const float* b_xyz, int64_t n0, int64_t n1, int64_t n2,
+                      int64_t nside, const int64_t* pix, int64_t count, int n_steps, int mode,
+                      float* maps, int nthreads) {
+  if (n0 < 1 || n1 < 1 || n2 < 1 || nside < 1 || n_steps < 1 || count < 0) return -1;
+  if (mode != OR_MODE_FP64 && mode != OR_MODE_REF16) return -1;
+  const int64_t npix = 12 * nside * nside;
+  for (int64_t i = 0; i < count; ++i)
+    if (pix[i] < 0 || pix[i] >= npix) return -1;
+  void* h = srto_fields_new(phi, b_xyz, n0, n1, n2, mode);
+  if (!h) return -3;
+  const int rc = srto_trace_pixels_h(h, nside, pix, count, n_steps, maps, nthreads);
+  srto_fields_delete(h);
+  return rc;
 }
 
 /* Trace RING pixels [pix_begin, pix_begin + pix_count). */

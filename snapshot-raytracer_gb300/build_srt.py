@@ -23,6 +23,8 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 LIBORACLE = os.path.join(ORACLE_DIR, "liboracle.so")
 REFERENCE_DIR = os.environ.get("SRT_REFERENCE_DIR", "/root/reference")
 LIBREF = os.path.join(ORACLE_DIR, "_ref", "libsrt_ref.so")
+LIBREFGPU = os.path.join(ORACLE_DIR, "librefgpu.so")
+REFCUBIN = os.path.join(ORACLE_DIR, "_ref", "ref_kernel.cubin")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -71,6 +73,9 @@ def build_oracle(verbose=False):
     _run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-c",
           os.path.join(ORACLE_DIR, "srt_oracle_tangent.cpp"), "-o", o2], verbose)
     _run(["g++", "-shared", "-fopenmp", "-o", LIBORACLE, o1, o2, "-lm"], verbose)
+    # loader of the reference's own GPU build (the cubin comes from build_ref.sh)
+    _run([NVCC, *GENCODE, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC",
+          os.path.join(ORACLE_DIR, "ref_gpu.cu"), "-o", LIBREFGPU], verbose)
     return LIBORACLE
 
 

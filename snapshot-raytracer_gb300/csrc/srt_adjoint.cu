@@ -92,6 +92,11 @@ __device__ __forceinline__ void load_vec(const T* base, int64_t count, int64_t s
 
 // ------------------------------------------------------------ MIXED mode
 
+// Floats of one step of the MIXED tape: the four stage inputs.
+constexpr int kTapeStep = 4 * 19;
+
+// PAIR: the forward steps read the row-pair field arrays (srt_fields.pr).
+template <bool PAIR>
 __global__ void __launch_bounds__(128) ckpt_kernel_mixed(const AdjArgs A) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= A.count) return;
@@ -104,7 +109,8 @@ __global__ void __launch_bounds__(128) ckpt_kernel_mixed(const AdjArgs A) {
   store_vec(ck, A.count, slot, y, kMixedState);
 #pragma unroll 1
   for (int st = 0; st < A.n_steps; ++st) {
-    step_mixed(R, A.F, A.G, x0, st, y, nullptr);
+    Guard gd;  // disabled: cell-face proximity matters for the maps, not for the gradient
+    step_mixed<PAIR>(R, A.F, A.G, x0, st, y, nullptr, 0, gd);
     const int done = st + 1;
     if (done % A.C == 0 || done == A.n_steps) {
       const int k = (done + A.C - 1) / A.C;
@@ -113,95 +119,116 @@ __global__ void __launch_bounds__(128) ckpt_kernel_mixed(const AdjArgs A) {
   }
 }
 
-template <typename Acc>
-__global__ void __launch_bounds__(128) reverse_kernel_mixed(const AdjArgs A, const Acc a0, const Acc a1,
-                                                           const Acc a2, const Acc a3) {
+// Cotangent of the final state from the map weights (the transpose of
+// extract_mixed) -> lam [19][count].
+__global__ void __launch_bounds__(128) final_cotangent_kernel_mixed(const AdjArgs A, float* lam) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= A.count) return;
-  const Acc acc[4] = {a0, a1, a2, a3};
   const int64_t ring = A.rays[slot];
   const int64_t o = ring - A.pix_begin;
   const RayDir d = ray_dir_pix(A.nside, ring);
   MixedRay R;
+  float y[kMixedState];
+  init_mixed(d, R, y);
+  load_vec((const float*)A.ckpt + (int64_t)A.nseg * kMixedState * A.count, A.count, slot, y, kMixedState);
+  float l[19];
+  for (int j = 0; j < 19; ++j) l[j] = 0.f;
+  float w[6];
+  for (int m = 0; m < 6; ++m) w[m] = A.w[m][o];
+  l[12] = w[0];
+  l[16] = w[1];
+  l[17] = w[2];
+  l[18] = w[3];
+  const float S = (float)A.n_steps;
+  float u[3];
+  for (int i = 0; i < 3; ++i) u[i] = (y[i] + y[19 + i]) / S;
+  const float q = R.eta[0] - 2.f * (R.n0[0] * u[0] + R.n0[1] * u[1] + R.n0[2] * u[2]) +
+                  (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+  const float c = rsqrt1p_m1(q);
+  const float r3 = (1.f + c) * (1.f + c) * (1.f + c);  // (1 + q)^(-3/2)
+  float Db[3], um[3];
+  for (int i = 0; i < 3; ++i) {
+    Db[i] = w[4] * R.a0[i] + w[5] * R.b0[i];
+    um[i] = u[i] - R.n0[i];
+  }
+  const float dotv = um[0] * Db[0] + um[1] * Db[1] + um[2] * Db[2];
+  for (int i = 0; i < 3; ++i) l[i] = ((1.f + c) * Db[i] - dotv * r3 * um[i]) / S;
+  store_vec(lam, A.count, slot, l, 19);
+}
+
+// Recompute segment sgi from its checkpoint, storing the four stage inputs
+// of every step: tape [C][4 x 19][count].
+template <bool PAIR>
+__global__ void __launch_bounds__(128, 2) segment_kernel_mixed(const AdjArgs A, int sgi) {
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= A.count) return;
+  const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
+  MixedRay R;
   float y[kMixedState], x0[3];
   mixed_observer(A.G, x0);
   init_mixed(d, R, y);
-  const float* ck = (const float*)A.ckpt;
-  float* sg = (float*)A.seg;
-  constexpr int kSeg = kMixedState + 57;
-  // cotangent of the final state from the map weights (inverse of extract_mixed)
-  float lam[19];
+  const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
+  load_vec((const float*)A.ckpt + (int64_t)sgi * kMixedState * A.count, A.count, slot, y, kMixedState);
+  float* tape = (float*)A.seg;
+#pragma unroll 1
+  for (int st = s0; st < s1; ++st) {
+    Guard gd;  // disabled
+    step_mixed<PAIR>(R, A.F, A.G, x0, st, y, tape + (int64_t)(st - s0) * kTapeStep * A.count + slot, A.count, gd);
+  }
+}
+
+// Backward sweep over segment sgi: per step, backwards, the RK4 adjoint
+//   a4 = J(u4)^T l/6, a3 = J(u3)^T (l/3 + a4), a2 = J(u2)^T (l/3 + a3/2),
+//   a1 = J(u1)^T (l/6 + a2/2), l <- l + a1 + a2 + a3 + a4,
+// with the stage inputs u from the tape; l carried in lam between segments.
+// l and the running sum of the a's live in shared memory (one column per
+// thread) to keep registers for the field passes.
+template <typename Acc, bool PAIR>
+__global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, int sgi, float* lam, const Acc a0,
+                                                           const Acc a1, const Acc a2, const Acc a3) {
+  __shared__ float s_lam[19][128];
+  __shared__ float s_tot[19][128];
+  const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= A.count) return;
+  const int t = threadIdx.x;
+  const Acc acc[4] = {a0, a1, a2, a3};
+  const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
+  MixedRay R;
+  float x0[3];
   {
-    load_vec(ck + (int64_t)A.nseg * kMixedState * A.count, A.count, slot, y, kMixedState);
-    for (int j = 0; j < 19; ++j) lam[j] = 0.f;
-    float w[6];
-    for (int m = 0; m < 6; ++m) w[m] = A.w[m][o];
-    lam[12] = w[0];
-    lam[16] = w[1];
-    lam[17] = w[2];
-    lam[18] = w[3];
-    const float S = (float)A.n_steps;
-    float u[3];
-    for (int i = 0; i < 3; ++i) u[i] = (y[i] + y[19 + i]) / S;
-    const float q = R.eta[0] - 2.f * (R.n0[0] * u[0] + R.n0[1] * u[1] + R.n0[2] * u[2]) +
-                    (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-    const float c = rsqrt1p_m1(q);
-    const float r3 = (1.f + c) * (1.f + c) * (1.f + c);  // (1 + q)^(-3/2)
-    float Db[3], um[3];
-    for (int i = 0; i < 3; ++i) {
-      Db[i] = w[4] * R.a0[i] + w[5] * R.b0[i];
-      um[i] = u[i] - R.n0[i];
-    }
-    const float dotv = um[0] * Db[0] + um[1] * Db[1] + um[2] * Db[2];
-    for (int i = 0; i < 3; ++i) lam[i] = ((1.f + c) * Db[i] - dotv * r3 * um[i]) / S;
+    float y[kMixedState];
+    init_mixed(d, R, y);
   }
+  mixed_observer(A.G, x0);
+  for (int j = 0; j < 19; ++j) s_lam[j][t] = lam[(int64_t)j * A.count + slot];
+  const float* tape = (const float*)A.seg;
+  const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
 #pragma unroll 1
-  for (int sgi = A.nseg - 1; sgi >= 0; --sgi) {
-    const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
-    load_vec(ck + (int64_t)sgi * kMixedState * A.count, A.count, slot, y, kMixedState);
+  for (int st = s1 - 1; st >= s0; --st) {
+    const float* rec = tape + (int64_t)(st - s0) * kTapeStep * A.count + slot;
+    for (int j = 0; j < 19; ++j) s_tot[j][t] = 0.f;
+    float an[19];  // a of the stage after this one
+    for (int j = 0; j < 19; ++j) an[j] = 0.f;
 #pragma unroll 1
-    for (int st = s0; st < s1; ++st) {
-      float* rec = sg + (int64_t)(st - s0) * kSeg * A.count;
-      store_vec(rec, A.count, slot, y, kMixedState);
-      float ks[57];
-      step_mixed(R, A.F, A.G, x0, st, y, ks);
-      store_vec(rec + (int64_t)kMixedState * A.count, A.count, slot, ks, 57);
-    }
-#pragma unroll 1
-    for (int st = s1 - 1; st >= s0; --st) {
-      const float* rec = sg + (int64_t)(st - s0) * kSeg * A.count;
-      float yi[kMixedState];
-      load_vec(rec, A.count, slot, yi, kMixedState);
-      float anext[19], atot[19];
-      for (int j = 0; j < 19; ++j) atot[j] = 0.f;
-#pragma unroll 1
-      for (int stage = 3; stage >= 0; --stage) {
-        // stage input u = y + c k_prev, c = 0, 1/2, 1/2, 1
-        float kprev[19], u[19], fb[19];
-        const float c = (stage == 0) ? 0.f : ((stage == 3) ? 1.f : 0.5f);
-        if (stage == 0) {
-          for (int j = 0; j < 19; ++j) kprev[j] = 0.f;
-        } else {
-          load_vec(rec + (int64_t)(kMixedState + 19 * (stage - 1)) * A.count, A.count, slot, kprev, 19);
-        }
-        mixed_stage(yi, kprev, c, u);
-        // output cotangent of this stage's k
-        const float wl = (stage == 0 || stage == 3) ? (1.f / 6.f) : (1.f / 3.f);
-        const float wa = (stage == 3) ? 0.f : ((stage == 2) ? 1.f : 0.5f);
-        for (int j = 0; j < 19; ++j) fb[j] = wl * lam[j] + (stage == 3 ? 0.f : wa * anext[j]);
-        StageView<float> V;
+    for (int stage = 3; stage >= 0; --stage) {
+      const float c = (stage == 0) ? 0.f : ((stage == 3) ? 1.f : 0.5f);
+      const float wl = (stage == 0 || stage == 3) ? (1.f / 6.f) : (1.f / 3.f);
+      const float wa = (stage == 3) ? 0.f : ((stage == 2) ? 1.f : 0.5f);
+      float fb[19];
+      for (int j = 0; j < 19; ++j) fb[j] = wl * s_lam[j][t] + wa * an[j];
+      StageView<float> V;
+      {
+        float u[19];
+        for (int j = 0; j < 19; ++j) u[j] = rec[(int64_t)(19 * stage + j) * A.count];
         stage_view_mixed(u, (float)st + c, R, A.G, x0, V);
-        float ub[19];
-        for (int j = 0; j < 19; ++j) ub[j] = 0.f;
-        rhs_vjp<float, Acc>(V, A.F, A.G, fb, ub, acc);
-        for (int j = 0; j < 19; ++j) {
-          anext[j] = ub[j];
-          atot[j] += ub[j];
-        }
       }
-      for (int j = 0; j < 19; ++j) lam[j] += atot[j];
+      for (int j = 0; j < 19; ++j) an[j] = 0.f;
+      rhs_vjp<float, Acc, PAIR>(V, A.F, A.G, fb, an, acc);
+      for (int j = 0; j < 19; ++j) s_tot[j][t] += an[j];
     }
+    for (int j = 0; j < 19; ++j) s_lam[j][t] += s_tot[j][t];
   }
+  for (int j = 0; j < 19; ++j) lam[(int64_t)j * A.count + slot] = s_lam[j][t];
 }
 
 // ------------------------------------------------------------- FP64 mode
@@ -304,12 +331,36 @@ __global__ void __launch_bounds__(128) reverse_kernel_fp64(const AdjArgs A, cons
 
 // ------------------------------------------------------------------ fold
 
+// Value of padded index q of an accumulator grid.
 template <typename G>
-__device__ __forceinline__ double fold_value(G v) { return (double)v; }
+struct PadRead;
 template <>
-__device__ __forceinline__ double fold_value<unsigned long long>(unsigned long long v) {
-  return (double)(long long)v / kFixedScale;
-}
+struct PadRead<double> {  // FP64 atomics: one entry per padded voxel
+  typedef double T;
+  const double* g;
+  __device__ T operator()(int64_t q) const { return g[q]; }
+  __device__ static double value(T s) { return s; }
+};
+template <>
+struct PadRead<unsigned long long> {  // fixed point: exact integer sums
+  typedef unsigned long long T;
+  const unsigned long long* g;
+  __device__ T operator()(int64_t q) const { return g[q]; }
+  __device__ static double value(T s) { return (double)(long long)s / kFixedScale; }
+};
+template <>
+struct PadRead<float4> {  // row-expanded FP32: taps of the rows starting at q, q-1, q-2, q-3
+  typedef float T;
+  const float4* g;
+  __device__ T operator()(int64_t q) const {
+    float s = g[q].x;
+    if (q >= 1) s += g[q - 1].y;
+    if (q >= 2) s += g[q - 2].z;
+    if (q >= 3) s += g[q - 3].w;
+    return s;
+  }
+  __device__ static double value(T s) { return (double)s; }
+};
 
 // For voxel (i, j, k): sum of the padded copies (the interior one and the
 // halo copies) -> out[v * stride + comp] (+= when accumulate).
@@ -318,6 +369,7 @@ __global__ void fold_kernel(const G* __restrict__ padded, int64_t n0, int64_t n1
                             int comp, int accumulate) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n0 * n1 * n2) return;
+  const PadRead<G> rd{padded};
   const int64_t i = v % n0, j = (v / n0) % n1, k = v / (n0 * n1);
   const int64_t p0 = n0 + 3, p1 = n1 + 3;
   int64_t pi[4], pj[4], pk[4];
@@ -335,11 +387,11 @@ __global__ void fold_kernel(const G* __restrict__ padded, int64_t n0, int64_t n1
   if (k == n2 - 1) pk[nk++] = 0;
   if (k == 0) pk[nk++] = n2 + 1;
   if (k == 1 % n2) pk[nk++] = n2 + 2;
-  G sum = 0;
+  typename PadRead<G>::T sum = 0;
   for (int a = 0; a < nk; ++a)
     for (int b = 0; b < nj; ++b)
-      for (int c = 0; c < ni; ++c) sum += padded[pi[c] + p0 * (pj[b] + p1 * pk[a])];
-  const float val = (float)fold_value<G>(sum);
+      for (int c = 0; c < ni; ++c) sum += rd(pi[c] + p0 * (pj[b] + p1 * pk[a]));
+  const float val = (float)PadRead<G>::value(sum);
   float* dst = out + v * stride + comp;
   *dst = accumulate ? *dst + val : val;
 }
@@ -407,11 +459,12 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
   int prev = 0;
   cudaGetDevice(&prev);
   if (prev != f->device) cudaSetDevice(f->device);
-  DevBuf counts, offsets, rays, wdev, ckpt, seg, gacc[4], gout_phi, gout_b;
+  DevBuf counts, offsets, rays, wdev, ckpt, seg, lam, gacc[4], gout_phi, gout_b;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int64_t kernels = 0, h2d = 0, d2h = 0;
   {
-    const size_t accsz = (determ || fp64) ? 8 : 4;
+    // padded accumulator entry: 8 B (FP64 / fixed point), 16 B (FP32 rows)
+    const size_t accsz = (determ || fp64) ? 8 : 16;
     if (!dev_io) {
       // host gradients: start from zero (or from the caller's values when accumulating)
       if (dphi) {
@@ -486,7 +539,9 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
       const int state = fp64 ? 19 : kMixedState;
       const size_t esz = fp64 ? sizeof(double) : sizeof(float);
       VJP_TRY(ckpt.alloc((size_t)(nseg + 1) * state * pix_count * esz), "cudaMalloc(checkpoints)");
-      VJP_TRY(seg.alloc((size_t)C * (state + 57) * pix_count * esz), "cudaMalloc(segment records)");
+      // per-step records of one segment: FP64 y, k1, k2, k3; MIXED the four stage inputs
+      VJP_TRY(seg.alloc((size_t)C * (fp64 ? state + 57 : kTapeStep) * pix_count * esz), "cudaMalloc(segment records)");
+      if (!fp64) VJP_TRY(lam.alloc((size_t)19 * pix_count * sizeof(float)), "cudaMalloc(state cotangents)");
       for (int fld = 0; fld < 4; ++fld) {
         const bool want = (fld == 3) ? (dphi != nullptr) : (db_xyz != nullptr);
         if (!want) continue;
@@ -525,18 +580,37 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
           reverse_kernel_fp64<AccF64><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
         }
       } else {
-        ckpt_kernel_mixed<<<blocks, 128, 0, s>>>(A);
-        if (determ) {
-          AccFixed ac[4];
-          make_acc<AccFixed, unsigned long long>(ac, A.acc);
-          reverse_kernel_mixed<AccFixed><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
-        } else {
-          AccF32 ac[4];
-          make_acc<AccF32, float>(ac, A.acc);
-          reverse_kernel_mixed<AccF32><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
+        // forward with checkpoints; then per segment, backwards: recompute
+        // the segment's tape, sweep it
+        const bool pair = f->pr[0] != nullptr;
+        if (pair)
+          ckpt_kernel_mixed<true><<<blocks, 128, 0, s>>>(A);
+        else
+          ckpt_kernel_mixed<false><<<blocks, 128, 0, s>>>(A);
+        final_cotangent_kernel_mixed<<<blocks, 128, 0, s>>>(A, (float*)lam.p);
+        kernels += 2;
+        AccF32 af[4];
+        AccFixed ax[4];
+        make_acc<AccF32, float4>(af, A.acc);
+        make_acc<AccFixed, unsigned long long>(ax, A.acc);
+        for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+          if (pair)
+            segment_kernel_mixed<true><<<blocks, 128, 0, s>>>(A, sgi);
+          else
+            segment_kernel_mixed<false><<<blocks, 128, 0, s>>>(A, sgi);
+          if (determ && pair)
+            sweep_kernel_mixed<AccFixed, true><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, ax[0], ax[1], ax[2], ax[3]);
+          else if (determ)
+            sweep_kernel_mixed<AccFixed, false><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, ax[0], ax[1], ax[2],
+                                                                      ax[3]);
+          else if (pair)
+            sweep_kernel_mixed<AccF32, true><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, af[0], af[1], af[2], af[3]);
+          else
+            sweep_kernel_mixed<AccF32, false><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, af[0], af[1], af[2], af[3]);
+          kernels += 2;
         }
       }
-      kernels += 2;
+      if (fp64) kernels += 2;
       VJP_TRY(cudaGetLastError(), "adjoint kernels");
       // ---- fold onto the periodic grid
       const unsigned fblocks = (unsigned)((vox + 255) / 256);
@@ -552,8 +626,8 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
           fold_kernel<double><<<fblocks, 256, 0, s>>>((const double*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
                                                      stride, comp, accum);
         else
-          fold_kernel<float><<<fblocks, 256, 0, s>>>((const float*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
-                                                    stride, comp, accum);
+          fold_kernel<float4><<<fblocks, 256, 0, s>>>((const float4*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
+                                                     stride, comp, accum);
         ++kernels;
       }
       VJP_TRY(cudaGetLastError(), "fold kernel");

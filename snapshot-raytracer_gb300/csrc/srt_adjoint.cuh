@@ -45,18 +45,27 @@ SRT_HD void cr_weights4(T t, CRW4<T>& c) {
 
 // ---------------------------------------------------------- accumulators
 
-// Where the tap cotangents go: a halo-padded gradient grid (same indexing as
-// the padded field). Three flavours: FP32 atomics, FP64 atomics, and 64-bit
-// fixed point (order-independent, so repeated runs give identical bits).
+// Where the tap cotangents go: one call per 4-tap x-row of a tricubic
+// footprint (padded index `row` of its first tap). Three flavours:
+//   AccF32    FP32 atomics into a row-expanded grid: entry r (a float4) holds
+//             the four tap contributions of rows starting at padded index r,
+//             so one 16-byte vector atomic carries a whole row; the fold
+//             kernel adds entry q.x + (q-1).y + (q-2).z + (q-3).w per voxel;
+//   AccF64    FP64 atomics into a halo-padded grid (one per tap);
+//   AccFixed  64-bit fixed point into a halo-padded grid (order-independent,
+//             so repeated runs give identical bits).
 // A null grid (gradient not requested) ignores the contributions.
 struct AccF32 {
-  float* g;
-  SRT_HD void add(int64_t i, float v) const {
+  float4* g;
+  SRT_HD void add_row(int64_t row, float c0, float c1, float c2, float c3) const {
     if (!g) return;
 #if defined(__CUDA_ARCH__)
-    atomicAdd(g + i, v);
+    atomicAdd(g + row, make_float4(c0, c1, c2, c3));
 #else
-    g[i] += v;
+    g[row].x += c0;
+    g[row].y += c1;
+    g[row].z += c2;
+    g[row].w += c3;
 #endif
   }
 };
@@ -64,12 +73,18 @@ struct AccF32 {
 struct AccF64 {
   double* g;
   SRT_HD void add(int64_t i, double v) const {
-    if (!g) return;
 #if defined(__CUDA_ARCH__)
     atomicAdd(g + i, v);
 #else
     g[i] += v;
 #endif
+  }
+  SRT_HD void add_row(int64_t row, double c0, double c1, double c2, double c3) const {
+    if (!g) return;
+    add(row, c0);
+    add(row + 1, c1);
+    add(row + 2, c2);
+    add(row + 3, c3);
   }
 };
 
@@ -82,13 +97,19 @@ constexpr double kFixedScale = 4294967296.0;
 struct AccFixed {
   unsigned long long* g;
   SRT_HD void add(int64_t i, double v) const {
-    if (!g) return;
     const long long q = llrint(v * kFixedScale);
 #if defined(__CUDA_ARCH__)
     atomicAdd(g + i, (unsigned long long)q);
 #else
     g[i] += (unsigned long long)q;
 #endif
+  }
+  SRT_HD void add_row(int64_t row, double c0, double c1, double c2, double c3) const {
+    if (!g) return;
+    add(row, c0);
+    add(row + 1, c1);
+    add(row + 2, c2);
+    add(row + 3, c3);
   }
 };
 
@@ -147,8 +168,8 @@ SRT_HD void tricubic_vjp(const float* __restrict__ f, int64_t base, int64_t px, 
       const T Cw = Z.w[c] * Aw[b] + Z.g[c] * Bw[b] + Z.h[c] * Dw[b];
       const T Cg = Z.w[c] * Ag[b] + Z.g[c] * Bg[b];
       const T Ch = Z.w[c] * Ah[b];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) acc.add(row + i, X.w[i] * Cw + X.g[i] * Cg + X.h[i] * Ch);
+      acc.add_row(row, X.w[0] * Cw + X.g[0] * Cg + X.h[0] * Ch, X.w[1] * Cw + X.g[1] * Cg + X.h[1] * Ch,
+                  X.w[2] * Cw + X.g[2] * Cg + X.h[2] * Ch, X.w[3] * Cw + X.g[3] * Cg + X.h[3] * Ch);
     }
     const T zw = Z.w[c], zg = Z.g[c], zh = Z.h[c], zk = Z.k[c];
     o000 += zw * s00; o001 += zg * s00; o002 += zh * s00; o003 += zk * s00;
@@ -181,6 +202,128 @@ SRT_HD void tricubic_vjp(const float* __restrict__ f, int64_t base, int64_t px, 
            qb[6] * o102 + qb[7] * o021 + qb[8] * o012 + qb[9] * o003;
 }
 
+// The same pass on the row-pair array (FP32 only): rows y and y+1 of a slice
+// arrive in one 64-bit load per x tap and every product runs on packed pairs
+// (two FP32 FMAs per instruction), as in tricubic_pair. basep: pair index of
+// voxel (cx-1, cy-1, cz-1); base: its index in the single layout, where the
+// tap cotangents go.
+template <typename Acc>
+SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64_t base, int64_t px, int64_t pxy,
+                              int64_t pxy2, float tx, float ty, float tz, const float* qb, Tri<float>& Q, float* xb,
+                              const Acc& acc) {
+  CRW4<float> X, Y, Z;
+  cr_weights4(tx, X);
+  cr_weights4(ty, Y);
+  cr_weights4(tz, Z);
+  float2 xw[4], xg[4], xh[4];
+  for (int i = 0; i < 4; ++i) {
+    xw[i] = dup2(X.w[i]);
+    xg[i] = dup2(X.g[i]);
+    xh[i] = dup2(X.h[i]);
+  }
+  // y weights and per-row scatter factors of rows (0, 1) and (2, 3)
+  float2 yw[2], yg[2], yh[2], yk[2], Aw[2], Bw[2], Dw[2], Ag[2], Bg[2], Ah[2];
+  for (int pr = 0; pr < 2; ++pr) {
+    const int b0 = 2 * pr, b1 = 2 * pr + 1;
+    yw[pr] = make_float2(Y.w[b0], Y.w[b1]);
+    yg[pr] = make_float2(Y.g[b0], Y.g[b1]);
+    yh[pr] = make_float2(Y.h[b0], Y.h[b1]);
+    yk[pr] = make_float2(Y.k[b0], Y.k[b1]);
+    Aw[pr] = ffma2(dup2(qb[0]), yw[pr], ffma2(dup2(qb[2]), yg[pr], fmul2(dup2(qb[7]), yh[pr])));
+    Bw[pr] = ffma2(dup2(qb[3]), yw[pr], fmul2(dup2(qb[8]), yg[pr]));
+    Dw[pr] = fmul2(dup2(qb[9]), yw[pr]);
+    Ag[pr] = ffma2(dup2(qb[1]), yw[pr], fmul2(dup2(qb[5]), yg[pr]));
+    Bg[pr] = fmul2(dup2(qb[6]), yw[pr]);
+    Ah[pr] = fmul2(dup2(qb[4]), yw[pr]);
+  }
+  float o000 = 0, o001 = 0, o002 = 0, o003 = 0, o010 = 0, o011 = 0, o012 = 0, o020 = 0, o021 = 0, o030 = 0;
+  float o100 = 0, o101 = 0, o102 = 0, o110 = 0, o111 = 0, o120 = 0, o200 = 0, o201 = 0, o210 = 0, o300 = 0;
+  const float2 z0 = make_float2(0.f, 0.f);
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c) {
+    float2 s00 = z0, s01 = z0, s02 = z0, s03 = z0, s10 = z0, s11 = z0, s12 = z0, s20 = z0, s21 = z0, s30 = z0;
+    const float2 zw = dup2(Z.w[c]), zg = dup2(Z.g[c]), zh = dup2(Z.h[c]);
+#pragma unroll
+    for (int pr = 0; pr < 2; ++pr) {
+      const float2* rp = f + basep + c * pxy2 + 2 * pr * px;
+      const float2 t0 = ldg(rp), t1 = ldg(rp + 1), t2 = ldg(rp + 2), t3 = ldg(rp + 3);
+      float2 r0 = fmul2(xw[0], t0), r1 = fmul2(xg[0], t0), r2 = fmul2(xh[0], t0), r3 = fmul2(dup2(X.k[0]), t0);
+      r0 = ffma2(xw[1], t1, r0);
+      r1 = ffma2(xg[1], t1, r1);
+      r2 = ffma2(xh[1], t1, r2);
+      r3 = ffma2(dup2(X.k[1]), t1, r3);
+      r0 = ffma2(xw[2], t2, r0);
+      r1 = ffma2(xg[2], t2, r1);
+      r2 = ffma2(xh[2], t2, r2);
+      r3 = ffma2(dup2(X.k[2]), t2, r3);
+      r0 = ffma2(xw[3], t3, r0);
+      r1 = ffma2(xg[3], t3, r1);
+      r2 = ffma2(xh[3], t3, r2);
+      r3 = ffma2(dup2(X.k[3]), t3, r3);
+      s00 = ffma2(yw[pr], r0, s00);
+      s01 = ffma2(yg[pr], r0, s01);
+      s02 = ffma2(yh[pr], r0, s02);
+      s03 = ffma2(yk[pr], r0, s03);
+      s10 = ffma2(yw[pr], r1, s10);
+      s11 = ffma2(yg[pr], r1, s11);
+      s12 = ffma2(yh[pr], r1, s12);
+      s20 = ffma2(yw[pr], r2, s20);
+      s21 = ffma2(yg[pr], r2, s21);
+      s30 = ffma2(yw[pr], r3, s30);
+      // tap cotangents of the two rows
+      const float2 Cw = ffma2(zw, Aw[pr], ffma2(zg, Bw[pr], fmul2(zh, Dw[pr])));
+      const float2 Cg = ffma2(zw, Ag[pr], fmul2(zg, Bg[pr]));
+      const float2 Ch = fmul2(zw, Ah[pr]);
+      float2 v[4];
+      for (int i = 0; i < 4; ++i) v[i] = ffma2(xw[i], Cw, ffma2(xg[i], Cg, fmul2(xh[i], Ch)));
+      const int64_t row = base + c * pxy + 2 * pr * px;
+      acc.add_row(row, v[0].x, v[1].x, v[2].x, v[3].x);
+      acc.add_row(row + px, v[0].y, v[1].y, v[2].y, v[3].y);
+    }
+    const float zwc = Z.w[c], zgc = Z.g[c], zhc = Z.h[c], zkc = Z.k[c];
+    const float S00 = s00.x + s00.y, S01 = s01.x + s01.y, S02 = s02.x + s02.y, S03 = s03.x + s03.y;
+    const float S10 = s10.x + s10.y, S11 = s11.x + s11.y, S12 = s12.x + s12.y;
+    const float S20 = s20.x + s20.y, S21 = s21.x + s21.y, S30 = s30.x + s30.y;
+    o000 += zwc * S00; o001 += zgc * S00; o002 += zhc * S00; o003 += zkc * S00;
+    o010 += zwc * S01; o011 += zgc * S01; o012 += zhc * S01;
+    o020 += zwc * S02; o021 += zgc * S02;
+    o030 += zwc * S03;
+    o100 += zwc * S10; o101 += zgc * S10; o102 += zhc * S10;
+    o110 += zwc * S11; o111 += zgc * S11;
+    o120 += zwc * S12;
+    o200 += zwc * S20; o201 += zgc * S20;
+    o210 += zwc * S21;
+    o300 += zwc * S30;
+  }
+  Q.v = o000;
+  Q.g[0] = o100;
+  Q.g[1] = o010;
+  Q.g[2] = o001;
+  Q.h[0] = o200;
+  Q.h[1] = o110;
+  Q.h[2] = o101;
+  Q.h[3] = o020;
+  Q.h[4] = o011;
+  Q.h[5] = o002;
+  xb[0] += qb[0] * o100 + qb[1] * o200 + qb[2] * o110 + qb[3] * o101 + qb[4] * o300 + qb[5] * o210 +
+           qb[6] * o201 + qb[7] * o120 + qb[8] * o111 + qb[9] * o102;
+  xb[1] += qb[0] * o010 + qb[1] * o110 + qb[2] * o020 + qb[3] * o011 + qb[4] * o210 + qb[5] * o120 +
+           qb[6] * o111 + qb[7] * o030 + qb[8] * o021 + qb[9] * o012;
+  xb[2] += qb[0] * o001 + qb[1] * o101 + qb[2] * o011 + qb[3] * o002 + qb[4] * o201 + qb[5] * o111 +
+           qb[6] * o102 + qb[7] * o021 + qb[8] * o012 + qb[9] * o003;
+}
+
+// One field's pass: the packed form on the row-pair array (PAIR, FP32 only)
+// or the plain one.
+template <bool PAIR, typename T, typename Acc>
+SRT_HD void field_pass(const float* f, const float2* fp, int64_t base, int64_t basep, const Geom& G, const T* t,
+                       const T* qb, Tri<T>& Q, T* xb, const Acc& acc) {
+  if constexpr (PAIR)
+    tricubic_vjp_pair<Acc>(fp, basep, base, G.px, G.pxy, G.pxy2, t[0], t[1], t[2], qb, Q, xb, acc);
+  else
+    tricubic_vjp<T, Acc>(f, base, G.px, G.pxy, t[0], t[1], t[2], qb, Q, xb, acc);
+}
+
 // -------------------------------------------------------- stage and core
 
 // What the right-hand-side vjp needs about one stage input, independent of
@@ -192,6 +335,7 @@ struct StageView {
   T A, Ap, s1, s2, e1, e2;
   bool branch;         // dA > 1/2
   int64_t base[4];     // padded base index per field: B_x, B_y, B_z, phi
+  int64_t basep[4];    // the same cells in the row-pair layout
   T t[4][3];           // cell offsets per field and axis
 };
 
@@ -206,7 +350,7 @@ SRT_HD T symv(const T* h, int i, int j) { return h[sym_idx(i, j)]; }
 // One B component's share of rhs_vjp: its cotangents (value, gradient,
 // Hessian) from the state-only intermediate cotangents, the fused pass, the
 // forward aggregates and its terms of the state cotangents.
-template <int C, typename T, typename Acc>
+template <int C, bool PAIR, typename T, typename Acc>
 SRT_HD void vjp_b_component(const StageView<T>& V, const FieldPtrs& F, const Geom& G, const T* fb, const T* ngBb, T e1b,
                             T e2b, T nlapb, const T* Tb, const Acc& acc, T* xb, T* nb, T* ab, T* bb, T* ngB, T& e1ngB,
                             T& e2ngB, T& nlap, T* Tm) {
@@ -227,7 +371,7 @@ SRT_HD void vjp_b_component(const StageView<T>& V, const FieldPtrs& F, const Geo
       qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
     }
   Tri<T> Q;
-  tricubic_vjp<T, Acc>(F.b[C], V.base[C], G.px, G.pxy, V.t[C][0], V.t[C][1], V.t[C][2], qb, Q, xb, acc);
+  field_pass<PAIR, T, Acc>(F.b[C], F.pr[C], V.base[C], V.basep[C], G, V.t[C], qb, Q, xb, acc);
   // forward aggregates
   for (int i = 0; i < 3; ++i) ngB[i] += Q.g[i] * nc;
   const T gn = Q.g[0] * n[0] + Q.g[1] * n[1] + Q.g[2] * n[2];
@@ -265,7 +409,7 @@ SRT_HD void vjp_b_component(const StageView<T>& V, const FieldPtrs& F, const Geo
 
 // yb += J(u)^T fb for the stage described by V; tap cotangents go to acc[0..3]
 // (B_x, B_y, B_z, phi).
-template <typename T, typename Acc>
+template <typename T, typename Acc, bool PAIR = false>
 SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, const T* fb, T* yb, const Acc* acc) {
   const T* n = V.n;
   const T* a = V.a;
@@ -325,11 +469,11 @@ SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, co
   T ngB[3] = {0, 0, 0}, e1ngB = 0, e2ngB = 0, nlap = 0, Tm[6] = {0, 0, 0, 0, 0, 0};
 
   // ---- B components (compile-time component index: no local-memory arrays)
-  vjp_b_component<0, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[0], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
+  vjp_b_component<0, PAIR, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[0], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
                              Tm);
-  vjp_b_component<1, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[1], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
+  vjp_b_component<1, PAIR, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[1], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
                              Tm);
-  vjp_b_component<2, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[2], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
+  vjp_b_component<2, PAIR, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[2], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
                              Tm);
 
   // ---- phi
@@ -343,7 +487,7 @@ SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, co
         const T m = Heb[sym_idx(i, j)] + (n[i] * n[j] - ((i == j) ? T(1) : T(0))) * PHb;
         qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
       }
-    tricubic_vjp<T, Acc>(F.phi, V.base[3], G.px, G.pxy, V.t[3][0], V.t[3][1], V.t[3][2], qb, P, xb, acc[3]);
+    field_pass<PAIR, T, Acc>(F.phi, F.pr[3], V.base[3], V.basep[3], G, V.t[3], qb, P, xb, acc[3]);
   }
   const T* g = P.g;
   for (int i = 0; i < 3; ++i) {
@@ -436,6 +580,7 @@ SRT_HD void stage_view_fp64(const double* y, const Geom& G, StageView<double>& V
       cell[i] = wrap64((int64_t)fl, G.n[i]);
     }
     V.base[f] = cell_base(G, cell[0], cell[1], cell[2]);
+    V.basep[f] = cell_base_pair(G, cell[0], cell[1], cell[2]);
   }
 }
 
@@ -480,6 +625,7 @@ SRT_HD void stage_view_mixed(const float* d, float s, const MixedRay& R, const G
       V.t[f][i] = stag ? ts[i] : tc[i];
     }
     V.base[f] = cell_base(G, cell[0], cell[1], cell[2]);
+    V.basep[f] = cell_base_pair(G, cell[0], cell[1], cell[2]);
   }
 }
 

@@ -228,6 +228,8 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
   const bool dev_out = (flags & SRT_OUTPUT_DEVICE) != 0;
   int rc = SRT_OK;
   float* dmaps = nullptr;
+  int64_t* refine_list = nullptr;
+  unsigned long long* refine_count = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int64_t kernels = 0;
   int prev = 0;
@@ -263,6 +265,16 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     a.pix_begin = pix_begin;
     a.pix_count = pix_count;
     a.n_steps = n_steps;
+    a.refine_list = nullptr;
+    a.refine_count = nullptr;
+    const bool refine = precision == SRT_PRECISION_MIXED && !(flags & SRT_MIXED_NO_REFINE);
+    if (refine) {
+      SRT_CUDA_TRY(cudaMallocAsync((void**)&refine_list, pix_count * sizeof(int64_t), s), "cudaMallocAsync(refine list)");
+      SRT_CUDA_TRY(cudaMallocAsync((void**)&refine_count, sizeof(unsigned long long), s), "cudaMallocAsync(refine count)");
+      SRT_CUDA_TRY(cudaMemsetAsync(refine_count, 0, sizeof(unsigned long long), s), "clear refine count");
+      a.refine_list = refine_list;
+      a.refine_count = refine_count;
+    }
     if (dev_out) {
       for (int m = 0; m < 6; ++m) a.maps[m] = maps[m];
     } else {
@@ -277,6 +289,7 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     }
     const int kmode = (precision == SRT_PRECISION_MIXED && f->pr[0]) ? kMIXED_PAIR : precision;
     SRT_CUDA_TRY(launch_trace(kmode, a, s, &kernels), "trace kernel launch");
+    if (refine) SRT_CUDA_TRY(launch_refine(a, s, &kernels), "refine kernel launch");
     if (timed) SRT_CUDA_TRY(cudaEventRecord(e1, s), "cudaEventRecord");
     if (!dev_out) {
       for (int m = 0; m < 6; ++m)
@@ -292,10 +305,18 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
       stats->ray_steps = pix_count * (int64_t)n_steps;
       stats->kernels = kernels;
       stats->d2h_bytes = dev_out ? 0 : 6 * pix_count * (int64_t)sizeof(float);
+      if (refine && timed) {
+        unsigned long long cnt = 0;
+        if (cudaMemcpy(&cnt, refine_count, sizeof(cnt), cudaMemcpyDeviceToHost) == cudaSuccess)
+          stats->refined_rays = (int64_t)cnt;
+      }
     }
   }
 fail:
   if (dmaps) cudaFree(dmaps);
+  // stream-ordered release: the refine kernel may still be queued (SRT_ASYNC)
+  if (refine_list) cudaFreeAsync(refine_list, s);
+  if (refine_count) cudaFreeAsync(refine_count, s);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (prev != f->device) cudaSetDevice(prev);

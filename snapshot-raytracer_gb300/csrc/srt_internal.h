@@ -34,6 +34,10 @@ struct TraceArgs {
   int64_t pix_begin, pix_count;
   int n_steps;
   float* maps[6];
+  // MIXED: rays that came within the cell-face guard are appended here
+  // (NULL: no fallback) and re-traced in FP64 by launch_refine.
+  int64_t* refine_list;
+  unsigned long long* refine_count;
 };
 
 Geom make_geom(const srt_fields* f);
@@ -47,6 +51,8 @@ cudaError_t launch_pair_build(const float* src, float2* dst, const int64_t pn[3]
 
 // Trace kernel launch (mode = kFP64 / kMIXED / kREF16).
 cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* kernels);
+// FP64 re-trace of the rays listed by a MIXED trace (count read on the device).
+cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels);
 
 // Peak issue-rate probes (FMA loop kernels); returns achieved FLOP/s.
 cudaError_t probe_fma(int kind, double* flops_per_s);

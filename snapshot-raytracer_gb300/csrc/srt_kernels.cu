@@ -10,6 +10,7 @@
 //                          pix2ang loop of :857-866)
 //   * fma_probe_kernel     FP32 / FP64 FMA issue-rate probe used for the roofline
 #include <cstdio>
+#include <algorithm>
 #include "srt_internal.h"
 
 namespace srt {
@@ -106,14 +107,127 @@ __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ?
   if (o < 0 || o >= A.pix_count) return;
   const RayDir d = ray_dir_pix(A.nside, ring);
   float out[6];
-  if (MODE == kMIXED_PAIR)
-    trace_ray_mixed<true>(A.F, A.G, d, A.n_steps, out);
-  else if (MODE == kMIXED)
-    trace_ray_mixed<false>(A.F, A.G, d, A.n_steps, out);
-  else
+  if (MODE == kMIXED_PAIR || MODE == kMIXED) {
+    __shared__ float guard_m[128][3];  // the ray's guard state, out of the register budget
+    const bool near = trace_ray_mixed<MODE == kMIXED_PAIR>(A.F, A.G, d, A.n_steps, out, guard_m[threadIdx.x]);
+    if (near && A.refine_list) {
+      const unsigned long long k = atomicAdd(A.refine_count, 1ull);
+      if (k < (unsigned long long)A.pix_count) A.refine_list[k] = o + A.pix_begin;
+    }
+  } else {
     trace_ray_std<MODE == kREF16 ? kREF16 : kFP64>(A.F, A.G, d, A.n_steps, out);
+  }
 #pragma unroll
   for (int m = 0; m < 6; ++m) A.maps[m][o] = out[m];
+}
+
+// FP64 re-trace of listed rays (MIXED rays near a cell face); the list's
+// length is read on the device, so no host round trip is needed.
+//
+// The rays are few (~0.1% of a sky) and FP64 runs at 1/64 of the FP32 rate.
+// A warp of 32 single-thread rays needs ~0.17 s for 512 steps however few of
+// its lanes are busy, and one such warp per SM sub-partition (608 on GB300)
+// already holds ~19k rays, so up to that count the launch takes one warp's
+// time. For fewer rays, each ray is traced by a group of four lanes, one per
+// field (B_x, B_y, B_z, phi): every lane interpolates its field, the group
+// exchanges the four results by shuffles, and every lane forms the rest of the
+// right-hand side with the operations of rhs_std<kFP64> in the same order, so
+// the maps are bit-identical to the FP64 trace while a warp issues about a
+// third of the FP64 instructions per step (~3x shorter). Four-lane groups win
+// up to about two warps per sub-partition; both kernels are launched and the
+// one not suited to the list's length returns at once.
+constexpr int64_t kRefineMaxBlocks = 152 * 32;
+constexpr int64_t kRefineGroupMaxRays = 2 * 608 * 8;
+
+__device__ __forceinline__ void shfl_tri(Tri<double>& d, const Tri<double>& s, int src, unsigned mask) {
+  d.v = __shfl_sync(mask, s.v, src);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) d.g[i] = __shfl_sync(mask, s.g[i], src);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) d.h[i] = __shfl_sync(mask, s.h[i], src);
+}
+
+// rhs_std<kFP64> with the four interpolations spread over a lane group
+// (field = lane & 3, group = the group's first lane, mask = live lanes).
+__device__ __forceinline__ void rhs_fp64_group(const double* y, double* dy, const FieldPtrs& F, const Geom& G,
+                                               int field, int group, unsigned mask) {
+  double n[3], a[3], b[3];
+  rhs_frame(y, n, a, b);
+  Tri<double> own;
+  {
+    const float* src = (field == 3) ? F.phi : ((field == 0) ? F.b[0] : ((field == 1) ? F.b[1] : F.b[2]));
+    const double ox = (field == 0) ? 0.5 : 0.0, oy = (field == 1) ? 0.5 : 0.0, oz = (field == 2) ? 0.5 : 0.0;
+    interp_std<double, float>(src, G, y[0] - ox, y[1] - oy, y[2] - oz, own);
+  }
+  BSums<double> B;
+  B.clear();
+  Tri<double> r;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    shfl_tri(r, own, group + c, mask);
+    B.add(c, r, n, a, b);
+  }
+  shfl_tri(r, own, group + 3, mask);
+  rhs_finish<double>(y, n, a, b, B, r, dy);
+}
+
+// step_std<kFP64> on rhs_fp64_group.
+__device__ __forceinline__ void step_fp64_group(const FieldPtrs& F, const Geom& G, double* y, int field, int group,
+                                                unsigned mask) {
+  double acc[19], k[19], ys[19];
+  for (int j = 0; j < 19; ++j) k[j] = 0.0;
+#pragma unroll 1
+  for (int st = 0; st < 4; ++st) {
+    const double c = (st == 3) ? 1.0 : 0.5;
+    for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
+    rhs_fp64_group(ys, k, F, G, field, group, mask);
+    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.0 * k[j] : acc[j]);
+  }
+  for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) / 6.0;
+}
+
+template <int LANES>
+__global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A) {
+  constexpr int kRays = 32 / LANES;  // rays per warp
+  const int lane = threadIdx.x;
+  const unsigned long long count = *A.refine_count;
+  const int64_t n = min((int64_t)count, A.pix_count);
+  if ((LANES == 4) != (n <= kRefineGroupMaxRays)) return;
+#pragma unroll 1
+  for (int64_t k0 = (int64_t)blockIdx.x * kRays; k0 < n; k0 += (int64_t)gridDim.x * kRays) {
+    const int64_t k = k0 + lane / LANES;
+    if (k >= n) continue;
+    const int64_t ring = A.refine_list[k];
+    const RayDir d = ray_dir_pix(A.nside, ring);
+    double y[19];
+    init_std(d, A.G, y);
+    if (LANES == 4) {
+      // live groups are a prefix of the warp: their lanes form the shuffle mask
+      const int64_t live = min((int64_t)kRays, n - k0);
+      const unsigned mask = (live >= kRays) ? 0xffffffffu : ((1u << (4 * live)) - 1u);
+#pragma unroll 1
+      for (int step = 0; step < A.n_steps; ++step) step_fp64_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
+    } else {
+#pragma unroll 1
+      for (int step = 0; step < A.n_steps; ++step) step_std<kFP64>(A.F, A.G, y, nullptr);
+    }
+    if (lane % LANES == 0) {
+      float out[6];
+      extract_std(d, A.G, y, out);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) A.maps[m][ring - A.pix_begin] = out[m];
+    }
+  }
+}
+
+cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels) {
+  const int64_t b1 = std::min((a.pix_count + 31) / 32, kRefineMaxBlocks);
+  const int64_t b4 = std::min((std::min(a.pix_count, kRefineGroupMaxRays) + 7) / 8, kRefineMaxBlocks);
+  if (b1 < 1) return cudaSuccess;
+  refine_kernel<4><<<(unsigned)b4, 32, 0, s>>>(a);
+  refine_kernel<1><<<(unsigned)b1, 32, 0, s>>>(a);
+  if (kernels) *kernels += 2;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* kernels) {

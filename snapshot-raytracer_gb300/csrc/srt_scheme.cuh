@@ -296,39 +296,34 @@ SRT_HD void interp_std(const TapT* f, const Geom& G, double x, double y, double 
 
 // --------------------------------------------- right-hand side, FP64 / REF16
 
-// 19-component right-hand side on the full state y (FP64 or REF16 arithmetic).
-// State: 0-2 x, 3-5 n, 6-8 e1, 9-11 e2, 12 dA, 13 dA', 14-15 sigma1/2,
-// 16-17 ellipticity1/2, 18 rotation (snapshot-raytracer.cu:317-335).
-template <int MODE>
-SRT_HD void rhs_std(const double* y, double* dy, const FieldPtrs& F, const Geom& G) {
-  typedef typename std::conditional<MODE == kREF16, float, double>::type IT;
-  double n[3], a[3], b[3];
-  {
-    const double rn = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
-    const double ra = sqrt(y[6] * y[6] + y[7] * y[7] + y[8] * y[8]);
-    const double rb = sqrt(y[9] * y[9] + y[10] * y[10] + y[11] * y[11]);
-    for (int i = 0; i < 3; ++i) {
-      n[i] = y[3 + i] / rn;
-      a[i] = y[6 + i] / ra;
-      b[i] = y[9 + i] / rb;
-    }
+// Unit vectors n, e1, e2 of the full state y (snapshot-raytracer.cu:338-349).
+SRT_HD void rhs_frame(const double* y, double* n, double* a, double* b) {
+  const double rn = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+  const double ra = sqrt(y[6] * y[6] + y[7] * y[7] + y[8] * y[8]);
+  const double rb = sqrt(y[9] * y[9] + y[10] * y[10] + y[11] * y[11]);
+  for (int i = 0; i < 3; ++i) {
+    n[i] = y[3 + i] / rn;
+    a[i] = y[6 + i] / ra;
+    b[i] = y[9 + i] / rb;
   }
-  // B contributions (snapshot-raytracer.cu:377-460): n.grad B, the e.n.grad B
-  // scalars, the tidal matrix and n . Laplacian B; the e_i.grad B vectors the
-  // reference also forms there are never used and are not computed.
-  IT bval[3], ngB[3] = {0, 0, 0}, e1ngB = 0, e2ngB = 0, nlap = 0;
-  IT T[6] = {0, 0, 0, 0, 0, 0};  // xx, xy, xz, yy, yz, zz
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    const double off[3] = {c == 0 ? 0.5 : 0.0, c == 1 ? 0.5 : 0.0, c == 2 ? 0.5 : 0.0};
-    Tri<IT> r;
-    if (MODE == kREF16) {
-      interp_std<IT, __half>(F.bh[c], G, y[0] - off[0], y[1] - off[1], y[2] - off[2], r);
-      tri_scale(r, (IT)(1.0 / 134217728.0));  // taps hold B * 2^27
-    } else {
-      interp_std<IT, float>(F.b[c], G, y[0] - off[0], y[1] - off[1], y[2] - off[2], r);
-    }
-    bval[c] = r.v;
+}
+
+// Sums over the B components of the right-hand side (snapshot-raytracer.cu:377-460):
+// n.grad B, the e.n.grad B scalars, the tidal matrix and n . Laplacian B.
+// The e_i.grad B vectors the reference also forms there are never used and
+// are not computed.
+template <typename IT>
+struct BSums {
+  IT val[3], ngB[3], e1ngB, e2ngB, nlap;
+  IT T[6];  // xx, xy, xz, yy, yz, zz
+  SRT_HD void clear() {
+    for (int i = 0; i < 3; ++i) ngB[i] = 0;
+    e1ngB = e2ngB = nlap = 0;
+    for (int i = 0; i < 6; ++i) T[i] = 0;
+  }
+  // Adds component c's value, gradient and Hessian r.
+  SRT_HD void add(int c, const Tri<IT>& r, const double* n, const double* a, const double* b) {
+    val[c] = r.v;
     for (int i = 0; i < 3; ++i) ngB[i] = (IT)(ngB[i] + r.g[i] * n[c]);
     const double gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
     const double ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
@@ -351,14 +346,18 @@ SRT_HD void rhs_std(const double* y, double* dy, const FieldPtrs& F, const Geom&
       }
     nlap = (IT)(nlap + (r.h[0] + r.h[3] + r.h[5]) * n[c]);
   }
-  Tri<IT> p;
-  interp_std<IT, float>(F.phi, G, y[0], y[1], y[2], p);
+};
 
+// The right-hand side from the frame, the B sums and phi's interpolation p
+// (snapshot-raytracer.cu:462-509).
+template <typename IT>
+SRT_HD void rhs_finish(const double* y, const double* n, const double* a, const double* b, const BSums<IT>& B,
+                       const Tri<IT>& p, double* dy) {
   const double dA = y[12], dAp = y[13], s1 = y[14], s2 = y[15], el1 = y[16], el2 = y[17];
   const double phi1 = 1.0 + 2.0 * p.v;
-  for (int i = 0; i < 3; ++i) dy[i] = -n[i] * phi1 - bval[i];
+  for (int i = 0; i < 3; ++i) dy[i] = -n[i] * phi1 - B.val[i];
   // -P_perp v with P_perp = n n^T - I  ->  v - n (n.v)
-  const double v0 = 2.0 * p.g[0] + ngB[0], v1 = 2.0 * p.g[1] + ngB[1], v2 = 2.0 * p.g[2] + ngB[2];
+  const double v0 = 2.0 * p.g[0] + B.ngB[0], v1 = 2.0 * p.g[1] + B.ngB[1], v2 = 2.0 * p.g[2] + B.ngB[2];
   const double nv = n[0] * v0 + n[1] * v1 + n[2] * v2;
   dy[3] = v0 - n[0] * nv;
   dy[4] = v1 - n[1] * nv;
@@ -366,20 +365,20 @@ SRT_HD void rhs_std(const double* y, double* dy, const FieldPtrs& F, const Geom&
   const double ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
   const double bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
   for (int i = 0; i < 3; ++i) {
-    dy[6 + i] = -2.0 * n[i] * ag - n[i] * e1ngB;
-    dy[9 + i] = -2.0 * n[i] * bg - n[i] * e2ngB;
+    dy[6 + i] = -2.0 * n[i] * ag - n[i] * B.e1ngB;
+    dy[9 + i] = -2.0 * n[i] * bg - n[i] * B.e2ngB;
   }
   const double L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
-                   0.25 * (n[0] * ngB[0] + n[1] * ngB[1] + n[2] * ngB[2]);
+                   0.25 * (n[0] * B.ngB[0] + n[1] * B.ngB[1] + n[2] * B.ngB[2]);
   // P_perp : H = n^T H n - tr H
   const double nHn = n[0] * n[0] * p.h[0] + n[1] * n[1] * p.h[3] + n[2] * n[2] * p.h[5] +
                      2.0 * (n[0] * n[1] * p.h[1] + n[0] * n[2] * p.h[2] + n[1] * n[2] * p.h[4]);
   const double PH = nHn - (p.h[0] + p.h[3] + p.h[5]);
   dy[12] = -dAp;
-  dy[13] = -4.0 * dAp * L - PH * dA + 0.5 * nlap * dA;
+  dy[13] = -4.0 * dAp * L - PH * dA + 0.5 * B.nlap * dA;
   // effective tidal matrix H + T/2 projected on the shear basis
   IT He[6];
-  for (int i = 0; i < 6; ++i) He[i] = (IT)(p.h[i] + 0.5 * T[i]);
+  for (int i = 0; i < 6; ++i) He[i] = (IT)(p.h[i] + 0.5 * B.T[i]);
   const double S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
                     (a[2] * a[2] - b[2] * b[2]) * He[5] +
                     2.0 * ((a[0] * a[1] - b[0] * b[1]) * He[1] + (a[0] * a[2] - b[0] * b[2]) * He[2] +
@@ -401,6 +400,33 @@ SRT_HD void rhs_std(const double* y, double* dy, const FieldPtrs& F, const Geom&
     dy[17] = 0.0;
     dy[18] = 0.0;
   }
+}
+
+// 19-component right-hand side on the full state y (FP64 or REF16 arithmetic).
+// State: 0-2 x, 3-5 n, 6-8 e1, 9-11 e2, 12 dA, 13 dA', 14-15 sigma1/2,
+// 16-17 ellipticity1/2, 18 rotation (snapshot-raytracer.cu:317-335).
+template <int MODE>
+SRT_HD void rhs_std(const double* y, double* dy, const FieldPtrs& F, const Geom& G) {
+  typedef typename std::conditional<MODE == kREF16, float, double>::type IT;
+  double n[3], a[3], b[3];
+  rhs_frame(y, n, a, b);
+  BSums<IT> B;
+  B.clear();
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    const double off[3] = {c == 0 ? 0.5 : 0.0, c == 1 ? 0.5 : 0.0, c == 2 ? 0.5 : 0.0};
+    Tri<IT> r;
+    if (MODE == kREF16) {
+      interp_std<IT, __half>(F.bh[c], G, y[0] - off[0], y[1] - off[1], y[2] - off[2], r);
+      tri_scale(r, (IT)(1.0 / 134217728.0));  // taps hold B * 2^27
+    } else {
+      interp_std<IT, float>(F.b[c], G, y[0] - off[0], y[1] - off[1], y[2] - off[2], r);
+    }
+    B.add(c, r, n, a, b);
+  }
+  Tri<IT> p;
+  interp_std<IT, float>(F.phi, G, y[0], y[1], y[2], p);
+  rhs_finish<IT>(y, n, a, b, B, p, dy);
 }
 
 // ------------------------------------------------------------ ray geometry
@@ -499,7 +525,8 @@ SRT_HD void two_sum(float a, float b, float& s, float& e) {
 }
 
 // Cell and offset along one axis for the position th + lo (th, lo floats,
-// their sum exact); the cell is chosen from the exact sum.
+// their sum exact); the cell is chosen from the exact sum. t is the offset
+// from the cell's lower face (it rounds to 1 within ~3e-8 of the upper face).
 SRT_HD void locate(float th, float lo, int n, float invn, int& cell, float& t) {
   const float fl = floorf(th);
   float s, e;
@@ -577,9 +604,56 @@ SRT_HD void add_b_component(const FieldPtrs& F, const Geom& G, const int* cc, co
 // Perturbation right-hand side g = f(y0(s) + d) - f(y0(s)) (FP32). `s` is the
 // affine parameter of the stage (step + 0, 1/2 or 1), d the stage state
 // (delta components in the layout of rhs_std), x0 the observer.
+// Cell-face guard. Catmull-Rom's Hessian jumps across cell faces, so where
+// the FP32 and FP64 trajectories pass a face on different sides the maps of
+// that ray differ by up to ~1% of their rms. The FP32 trajectory's distance
+// from the FP64 one was measured on the GPU, stage by stage (256^3 and 512^3
+// Gaussian fields, 256 steps, 295k rays), against the running maxima of the
+// perturbation, Mx = max |dx| and Mn = max |dn| over the path so far:
+// |x32 - x64| <= k (Mx + s Mn) with k below 8e-8 for half the rays, below
+// 2e-7 for 99% and below 3.7e-7 for all. A stage whose position lies within
+// g = kFaceGuardRel (Mx + s Mn) + kFaceGuardAbs of a cell face (either face,
+// centred or staggered grid) marks the ray for an FP64 re-trace.
+constexpr float kFaceGuardRel = 4e-7f;
+constexpr float kFaceGuardAbs = 1e-10f;
+// No guard is needed for the dA > 1/2 switch (snapshot-raytracer.cu:497): dA
+// passes 1/2 inside the first step, where dA - 1/2 at the midpoint stages is
+// either exactly 0 in both precisions (the switch is off in both) or ~k2/2 ~
+// n.grad phi ~ 1e-5 with a relative FP32 error ~1e-7, so the two agree on its
+// sign; and were they to differ, the switched terms are proportional to the
+// shear, which is 0 at the start of the ray.
+
+// Per-ray guard state: the flag, and (through m, three floats the caller
+// provides; the trace kernel keeps them in shared memory, out of the register
+// budget) the running maxima Mx = max |dx| and Mn = max |dn| taken at the
+// start of each step and the smallest distance dmin of the step's stage
+// positions from a cell face. A step is flagged when
+// dmin < kFaceGuardRel (Mx + s_end Mn) + kFaceGuardAbs, s_end the step's end.
+// Guard{} (m null) is disabled.
+struct Guard {
+  bool near = false;
+  float* m = nullptr;
+  SRT_HD void begin_step(const float* y) {
+    m[0] = fmaxf(m[0], fmaxf(fabsf(y[0]), fmaxf(fabsf(y[1]), fabsf(y[2]))));
+    m[1] = fmaxf(m[1], fmaxf(fabsf(y[3]), fmaxf(fabsf(y[4]), fabsf(y[5]))));
+    m[2] = 1.f;
+  }
+  // a stage's smallest distance from a face
+  SRT_HD void face(float d) {
+    if (m) m[2] = fminf(m[2], d);
+  }
+  SRT_HD void end_step(int step) {
+    near |= m[2] < kFaceGuardRel * (m[0] + (float)(step + 1) * m[1]) + kFaceGuardAbs;
+  }
+};
+
+// Distance of offset t from the nearer face; 1 - t is 0 where t rounded to 1
+// (within ~3e-8 of the upper face), which errs on the side of flagging.
+SRT_HD float face_dist(float t) { return fminf(t, 1.f - t); }
+
 template <bool PAIR>
 SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtrs& F, const Geom& G,
-                      const float* x0, float* g) {
+                      const float* x0, float* g, Guard& gd) {
   float Dn[3], Da[3], Db[3];
   unit_pert(R.n0, d + 3, R.eta[0], Dn);
   unit_pert(R.a0, d + 6, R.eta[1], Da);
@@ -602,6 +676,8 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
     locate(th, lo, G.n[i], G.invn[i], cc[i], tc[i]);          // centred
     locate(th - 0.5f, lo, G.n[i], G.invn[i], cs[i], ts[i]);   // staggered by -1/2
   }
+  gd.face(fminf(fminf(fminf(face_dist(tc[0]), face_dist(ts[0])), fminf(face_dist(tc[1]), face_dist(ts[1]))),
+                fminf(face_dist(tc[2]), face_dist(ts[2]))));
   CRW<float> Cx, Cy, Cz;  // centred weights, shared by phi and two axes of each B component
   cr_weights(tc[0], Cx);
   cr_weights(tc[1], Cy);
@@ -715,11 +791,14 @@ SRT_HD void mixed_stage(const float* y, const float* k, float c, float* ys) {
   for (int j = kCompensated; j < 19; ++j) ys[j] = y[j] + c * k[j];
 }
 
-// One RK4 step from affine parameter `step`; when ks is given, the stage
-// derivatives k1, k2, k3 are stored there (3 x 19).
+// One RK4 step from affine parameter `step`; when us is given, the four stage
+// inputs (the perturbation states the right-hand side is evaluated at, with
+// the compensations folded in) are stored there: component j of stage st at
+// us[(19 st + j) * stride]. gd.near is set when a stage of the step came
+// within the guards above.
 template <bool PAIR = false>
 SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, const float* x0, int step, float* y,
-                       float* ks) {
+                       float* us, int64_t stride, Guard& gd) {
   float k[19], acc[19], ys[19];
   for (int j = 0; j < 19; ++j) k[j] = 0.f;
   const float s0 = (float)step;
@@ -727,9 +806,12 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
   for (int st = 0; st < 4; ++st) {
     const float c = (st == 0) ? 0.f : ((st == 3) ? 1.f : 0.5f);
     mixed_stage(y, k, c, ys);
-    rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k);
-    if (ks && st < 3)
-      for (int j = 0; j < 19; ++j) ks[19 * st + j] = k[j];
+    if (us)
+      for (int j = 0; j < 19; ++j) us[(19 * st + j) * stride] = ys[j];
+    rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k, gd);
+    // at s = 0 the ray sits exactly on the observer (a grid node, offsets
+    // exactly 0) in both precisions, so no cell choice can differ there
+    if (step == 0 && st == 0 && gd.m) gd.m[2] = 1.f;
     for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
   }
   for (int j = 0; j < kCompensated; ++j) {
@@ -763,15 +845,26 @@ SRT_HD void extract_mixed(const MixedRay& R, int n_steps, const float* y, float 
   out[3] = y[18];
 }
 
+// Returns true when the ray came within the guards (its FP64 trace may
+// differ by a cell choice; the caller re-traces it in FP64).
 template <bool PAIR = false>
-SRT_HD void trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6]) {
+SRT_HD bool trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, int n_steps, float out[6],
+                            float* guard_m) {
   MixedRay R;
   float y[kMixedState], x0[3];
   mixed_observer(G, x0);
   init_mixed(d, R, y);
+  Guard gd;
+  gd.m = guard_m;
+  gd.m[0] = gd.m[1] = 0.f;
 #pragma unroll 1
-  for (int step = 0; step < n_steps; ++step) step_mixed<PAIR>(R, F, G, x0, step, y, nullptr);
+  for (int step = 0; step < n_steps; ++step) {
+    gd.begin_step(y);
+    step_mixed<PAIR>(R, F, G, x0, step, y, nullptr, 0, gd);
+    gd.end_step(step);
+  }
   extract_mixed(R, n_steps, y, out);
+  return gd.near;
 }
 
 // Ray direction of a RING pixel centre (FP64: cos/sin of the colatitude from

@@ -26,6 +26,7 @@ SRT_ASYNC = 4
 SRT_ACCUMULATE = 8
 SRT_DETERMINISTIC = 16
 SRT_FIELDS_NO_PAIRS = 32
+SRT_MIXED_NO_REFINE = 64
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
           -5: "format error", -6: "no CUDA device", -7: "unsupported"}
@@ -40,7 +41,7 @@ class SrtError(RuntimeError):
 class Stats(ctypes.Structure):
     _fields_ = [("trace_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("rays", ctypes.c_int64),
                 ("ray_steps", ctypes.c_int64), ("kernels", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64)]
+                ("d2h_bytes", ctypes.c_int64), ("refined_rays", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -195,7 +196,7 @@ class Fields:
         self.close()
 
     def forward(self, nside, n_steps, pix_begin=0, pix_count=None, precision="mixed", out=None, stream=None,
-                async_=False):
+                async_=False, refine=True):
         """Six maps of RING pixels [pix_begin, pix_begin + pix_count).
         out: None (returns a new (6, count) float32 numpy array), a (6, count)
         numpy array, or a (6, count) CUDA tensor (device output). Returns
@@ -210,28 +211,37 @@ class Fields:
             raise ValueError("out must have shape (6, %d)" % pix_count)
         rows = _FP6(*[p + m * pix_count * 4 for m in range(6)])
         st = Stats()
-        flags = (SRT_OUTPUT_DEVICE if dev else 0) | (SRT_ASYNC if async_ else 0)
+        flags = (SRT_OUTPUT_DEVICE if dev else 0) | (SRT_ASYNC if async_ else 0) | \
+            (0 if refine else SRT_MIXED_NO_REFINE)
         _check(lib().srt_forward(self._h, nside, pix_begin, pix_count, n_steps, PRECISION[precision], rows, flags,
                                  _stream_ptr(stream), ctypes.byref(st)))
         return out, st
 
     def vjp(self, nside, n_steps, weights, pix_begin=0, pix_count=None, precision="mixed", dphi=None, db_xyz=None,
-            ckpt_every=0, accumulate=False, deterministic=False, stream=None):
+            ckpt_every=0, accumulate=False, deterministic=False, stream=None, wrt=("phi", "b")):
         """Gradient of sum(weights * maps) w.r.t. phi and B (srt_vjp).
         weights: (6, count) float32 (numpy or CUDA tensor). dphi / db_xyz:
         outputs shaped like phi / b_xyz (numpy or CUDA tensors); new numpy
-        arrays when None. Returns (dphi, db_xyz, Stats)."""
+        arrays when None. wrt: which gradients to form ("phi", "b"); the other
+        is neither computed nor returned (None). Returns (dphi, db_xyz, Stats)."""
         npix = 12 * nside * nside
         if pix_count is None:
             pix_count = npix - pix_begin
+        wrt = tuple(wrt)
+        if not wrt or any(w not in ("phi", "b") for w in wrt):
+            raise ValueError("wrt must name 'phi' and/or 'b', got %r" % (wrt,))
         n0, n1, n2 = self.n
-        if dphi is None:
+        if "phi" not in wrt:
+            dphi = None
+        elif dphi is None:
             dphi = np.zeros((n2, n1, n0), np.float32)
-        if db_xyz is None:
+        if "b" not in wrt:
+            db_xyz = None
+        elif db_xyz is None:
             db_xyz = np.zeros((n2, n1, n0, 3), np.float32)
         pw, wdev = _ptr(weights, False)
-        pg, gdev = _ptr(dphi, False)
-        pb, bdev = _ptr(db_xyz, False)
+        pg, gdev = _ptr(dphi, False) if dphi is not None else (None, wdev)
+        pb, bdev = _ptr(db_xyz, False) if db_xyz is not None else (None, wdev)
         if not (wdev == gdev == bdev):
             raise ValueError("weights and gradients must all be host or all be device buffers")
         rows = _FP6(*[pw + m * pix_count * 4 for m in range(6)])

@@ -1,9 +1,13 @@
-"""Pixel-range sharding of the forward across processes (one GPU each).
+"""Pixel-range sharding of the forward and of the vjp across processes (one
+GPU each).
 
 Rays are independent, so a sky (or the reference's batch range) splits into
 contiguous RING ranges with no communication during the trace; the only
 exchange is assembling the maps afterwards, which the reference leaves to the
 user (it writes one file per batch, snapshot-raytracer.cu:708-717, :939-987).
+The vjp of a loss summed over pixels splits the same way: each rank forms the
+gradient of its pixels' share (its slice of the weights) and one sum
+all-reduce of the gradient grids gives the full gradient.
 """
 import numpy as np
 
@@ -47,3 +51,31 @@ def gather_maps(part, pix_begin, pix_count, group=None):
     else:
         dist.all_gather(bufs, t, group=group)
     return assemble([b.numpy() for b in bufs], pix_begin, pix_count, world)
+
+
+def shard_weights(weights, pix_begin, pix_count, rank, world):
+    """The (6, count_r) slice of (6, pix_count) map weights for `rank`'s range,
+    with that range: (weights_r, begin_r, count_r)."""
+    b, c = shard_range(pix_begin, pix_count, rank, world)
+    return np.ascontiguousarray(weights[:, b - pix_begin:b - pix_begin + c]), b, c
+
+
+def allreduce_gradients(grads, group=None):
+    """Sum all-reduce, in place, of the ranks' gradient grids (torch tensors:
+    CUDA with NCCL, CPU with gloo; numpy arrays go through a CPU tensor)."""
+    import torch
+    import torch.distributed as dist
+
+    out = []
+    for g in grads:
+        if g is None:
+            out.append(None)
+            continue
+        if isinstance(g, np.ndarray):
+            t = torch.from_numpy(g)
+            dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+            out.append(t.numpy())
+        else:
+            dist.all_reduce(g, op=dist.ReduceOp.SUM, group=group)
+            out.append(g)
+    return out

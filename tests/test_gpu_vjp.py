@@ -125,6 +125,13 @@ def test_vjp_accumulate_phi_only_and_ranges(srt):
         rows = (ctypes.c_void_p * 6)(*[w.ctypes.data + 4 * w.shape[1] * m for m in range(6)])
         rc = srt.lib().srt_vjp(f.handle, nside, 0, 48, steps, 0, rows, gphi.ctypes.data, None, 0, 16, None, None)
         assert rc == 0 and np.array_equal(gphi.view(np.uint32), g1.view(np.uint32))
+        # the same through the Python face (wrt), in the MIXED deterministic mode
+        gp_only, gb_none, _ = f.vjp(nside, steps, w, precision="mixed", deterministic=True, wrt=("phi",))
+        gfull, _, _ = f.vjp(nside, steps, w, precision="mixed", deterministic=True)
+        assert gb_none is None and np.array_equal(gp_only.view(np.uint32), gfull.view(np.uint32))
+        gp_none, gb_only, _ = f.vjp(nside, steps, w, precision="mixed", deterministic=True, wrt=("b",))
+        _, gbfull, _ = f.vjp(nside, steps, w, precision="mixed", deterministic=True)
+        assert gp_none is None and np.array_equal(gb_only.view(np.uint32), gbfull.view(np.uint32))
         # disjoint pixel ranges add up to the full-sky gradient
         acc = np.zeros_like(phi)
         for lo, hi in ((0, 13), (13, 40), (40, 48)):
