@@ -152,6 +152,23 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
                 int n_steps, int precision, float* const maps[SRT_NUM_MAPS], unsigned flags,
                 void* stream, srt_stats* stats);
 
+/* Forward trace that allocates no device memory, for callers that cannot
+ * allocate when they trace: applications whose device memory is reserved up
+ * front by their own pool (a fresh cudaMalloc fails there) and loops that
+ * cannot take the device-wide synchronisation a cudaMalloc / cudaFree may
+ * imply. Same arguments and results as srt_forward with SRT_OUTPUT_DEVICE
+ * (maps are device buffers of pix_count floats each), MIXED or FP64. The
+ * scratch (the list of rays MIXED re-traces in FP64) lives in a file-scope
+ * device array of 2^20 ray indices (8 MiB) that every GPU loading the library
+ * holds until exit, so one call traces at most 2^20 rays; larger ranges are
+ * rejected with SRT_ERR_INVALID_ARGUMENT. The first call on a device looks up
+ * the array's address (make it before any stream capture). Calls share the
+ * array: calls whose work overlaps on the GPU race. Synchronous unless
+ * SRT_ASYNC. No counterpart in the reference (it has no library API). */
+int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
+                        int n_steps, int precision, float* const maps[SRT_NUM_MAPS], unsigned flags,
+                        void* stream);
+
 /* ------------------------------------------------------------------ vjp */
 
 /* Gradient of L = sum_m sum_p weights[m][p] * maps[m][p] (maps as produced by

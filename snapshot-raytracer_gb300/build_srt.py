@@ -28,7 +28,7 @@ REFCUBIN = os.path.join(ORACLE_DIR, "_ref", "ref_kernel.cubin")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-CUDA_SOURCES = ["srt_kernels.cu", "srt_adjoint.cu", "srt_api.cu"]
+CUDA_SOURCES = ["srt_kernels.cu", "srt_adjoint.cu", "srt_api.cu", "srt_noalloc.cu"]
 HOST_SOURCES = ["srt_io.cpp"]
 
 
