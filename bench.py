@@ -74,7 +74,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--oracle-sample", type=int, default=24, help="pixels checked against the FP64 oracle")
     ap.add_argument("--adjoint", default="256,128,128,12",
-                    help="adjoint leg: grid,nside,n_steps,ckpt_every ('' to skip)")
+                    help="adjoint leg: grid,nside,n_steps,ckpt_every[,phi] ('' to skip; phi: w.r.t. phi only)")
     return ap.parse_args()
 
 
@@ -211,31 +211,38 @@ def time_cpu(fn, target_s, make_sample, start=16):
 
 def run_adjoint_leg(spec, seed, dev):
     """Mixed forward vs mixed vjp (loss = sum of seeded N(0,1) pixel weights x
-    maps) at grid,nside,n_steps with checkpoints every ckpt_every steps; the
-    gradient is checked against the deterministic FP64 vjp (whole grid) and, on
-    a 64-pixel range, against the oracle's FP64 forward-mode tangent."""
+    maps) at grid,nside,n_steps with checkpoints every ckpt_every steps
+    (spec "grid,nside,n_steps,ckpt_every[,phi]"; phi: gradient w.r.t. phi
+    only). Up to 256^3 the gradient is checked against the deterministic FP64
+    vjp (whole grid) and, on a 64-pixel range, against the oracle's FP64
+    forward-mode tangent."""
     import torch
 
     import srt
     import srt_fields
     from oracle import oracle
 
-    n, nside, S, C = [int(x) for x in spec.split(",")]
+    parts = spec.split(",")
+    n, nside, S, C = [int(x) for x in parts[:4]]
+    wrt = ("phi",) if len(parts) > 4 and parts[4] == "phi" else ("phi", "b")
     npix = 12 * nside * nside
     phi, b = srt_fields.gaussian_fields_torch(n, seed=seed + 101, device=dev)
     w = torch.from_numpy(np.random.default_rng(seed).standard_normal((6, npix)).astype(np.float32)).to(dev)
     out = torch.empty((6, npix), dtype=torch.float32, device=dev)
     gphi = torch.zeros_like(phi)
-    gb = torch.zeros_like(b)
+    gb = torch.zeros_like(b) if "b" in wrt else None
     stream = torch.cuda.current_stream(dev)
-    res = {"workload": "%d^3, nside %d (%d rays), %d steps, checkpoints every %d steps" % (n, nside, npix, S, C)}
+    res = {"workload": "%d^3, nside %d (%d rays), %d steps, checkpoints every %d steps, gradient w.r.t. %s" %
+                       (n, nside, npix, S, C, " and ".join(wrt))}
+    reps = 4 if n <= 512 else 2
     with srt.Fields(phi, b, stream=stream) as f:
         fwd, adj = [], []
         fwd_nr = []
-        for i in range(4):
+        for i in range(reps):
             _, st = f.forward(nside, S, precision="mixed", out=out, stream=stream)
             _, st2 = f.forward(nside, S, precision="mixed", out=out, stream=stream, refine=False)
-            _, _, sa = f.vjp(nside, S, w, precision="mixed", dphi=gphi, db_xyz=gb, ckpt_every=C, stream=stream)
+            _, _, sa = f.vjp(nside, S, w, precision="mixed", dphi=gphi, db_xyz=gb, ckpt_every=C, stream=stream,
+                             wrt=wrt)
             if i > 0:
                 fwd.append(st.trace_ms)
                 fwd_nr.append(st2.trace_ms)
@@ -246,6 +253,11 @@ def run_adjoint_leg(spec, seed, dev):
         res["vjp_over_forward"] = res["vjp_ms"] / res["forward_ms"]
         res["vjp_over_fp32_forward"] = res["vjp_ms"] / res["forward_fp32_only_ms"]
         res["vjp_ray_steps_per_s"] = npix * S / (res["vjp_ms"] * 1e-3)
+        if n > 256 or "b" not in wrt:
+            torch.cuda.synchronize()
+            del phi, b, gphi, gb, out, w
+            torch.cuda.empty_cache()
+            return res
         # accuracy: mixed vjp vs deterministic FP64 vjp over the whole grid
         g64 = torch.zeros_like(phi)
         b64 = torch.zeros_like(b)
@@ -312,6 +324,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
     fields = srt.Fields(phi_d, b_d, stream=stream)
+    if args.e2e_steps <= 0:  # the laid-out copy is all the trace needs (2048^3: 137 GB freed)
+        torch.cuda.synchronize()
+        del phi_d, b_d
+        torch.cuda.empty_cache()
     out = torch.empty((6, npix), dtype=torch.float32, device=dev)
 
     peak_fp32 = srt.probe_peak("fp32")
@@ -349,14 +365,16 @@ def run_ours(args):
               ("f64" if args.precision == "fp64" else "f32/f16"), "data": "synthetic", "config": cfg,
               "gpu_launches": kernels,
               "refined_rays_per_step": int(np.max(refined)) if refined else 0}
+    # DRAM bytes of one trace launch, from an ncu capture of this workload
+    # (profiles/trace_traffic.json); null for workloads that were not captured
     traffic = None
     prof = os.path.join(ROOT, "profiles", "trace_traffic.json")
     if os.path.isfile(prof):
         try:
-            per = json.load(open(prof)).get("dram_bytes_per_ray_step", {}).get(args.precision)
-            if per is not None:
-                traffic = per * ray_steps
-        except (OSError, ValueError):
+            rec = json.load(open(prof)).get("dram_bytes_per_launch", {}).get(args.precision)
+            if rec and (rec["grid"], rec["nside"], rec["n_steps"]) == (n, nside, S):
+                traffic = rec["read"] + rec["write"]
+        except (OSError, ValueError, KeyError):
             traffic = None
     result["roofline"] = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak_fp32 / 1e12,
                           "unit": "TFLOP/s", "frac": achieved / peak_fp32, "traffic": traffic,

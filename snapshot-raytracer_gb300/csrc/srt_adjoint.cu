@@ -92,6 +92,7 @@ __device__ __forceinline__ void load_vec(const T* base, int64_t count, int64_t s
 
 // ------------------------------------------------------------ MIXED mode
 
+
 // Floats of one step of the MIXED tape: the four stage inputs.
 constexpr int kTapeStep = 4 * 19;
 
@@ -180,9 +181,50 @@ __global__ void __launch_bounds__(128, 2) segment_kernel_mixed(const AdjArgs A, 
 // Backward sweep over segment sgi: per step, backwards, the RK4 adjoint
 //   a4 = J(u4)^T l/6, a3 = J(u3)^T (l/3 + a4), a2 = J(u2)^T (l/3 + a3/2),
 //   a1 = J(u1)^T (l/6 + a2/2), l <- l + a1 + a2 + a3 + a4,
-// with the stage inputs u from the tape; l carried in lam between segments.
-// l and the running sum of the a's live in shared memory (one column per
-// thread) to keep registers for the field passes.
+// with the stage inputs u from the tape (the next stage's inputs are loaded
+// while the current stage runs); l carried in lam between segments. l and the
+// running sum of the a's live in shared memory (one column per thread) to keep
+// registers for the field passes.
+template <typename Acc, bool PAIR>
+__device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t slot, const MixedRay& R,
+                                              const float* x0, float* lam, const Acc* acc, float (*s_lam)[128],
+                                              float (*s_tot)[128]) {
+  const int t = threadIdx.x;
+  for (int j = 0; j < 19; ++j) s_lam[j][t] = lam[(int64_t)j * A.count + slot];
+  const float* tape = (const float*)A.seg + slot;
+  const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
+  // flattened (step, stage) index, descending; u holds the stage inputs of q
+  int q = (s1 - s0) * 4 - 1;
+  float u[19];
+  for (int j = 0; j < 19; ++j) u[j] = tape[((int64_t)(q >> 2) * kTapeStep + 19 * (q & 3) + j) * A.count];
+  float an[19];  // a of the stage after this one
+#pragma unroll 1
+  for (; q >= 0; --q) {
+    const int st = s0 + (q >> 2), stage = q & 3;
+    if (stage == 3) {
+      for (int j = 0; j < 19; ++j) s_tot[j][t] = 0.f;
+      for (int j = 0; j < 19; ++j) an[j] = 0.f;
+    }
+    const float c = (stage == 0) ? 0.f : ((stage == 3) ? 1.f : 0.5f);
+    const float wl = (stage == 0 || stage == 3) ? (1.f / 6.f) : (1.f / 3.f);
+    const float wa = (stage == 3) ? 0.f : ((stage == 2) ? 1.f : 0.5f);
+    float fb[19];
+    for (int j = 0; j < 19; ++j) fb[j] = wl * s_lam[j][t] + wa * an[j];
+    StageView<float> V;
+    stage_view_mixed(u, (float)st + c, R, A.G, x0, V);
+    if (q > 0) {  // prefetch the next (earlier) stage's inputs
+      const int qn = q - 1;
+      for (int j = 0; j < 19; ++j) u[j] = tape[((int64_t)(qn >> 2) * kTapeStep + 19 * (qn & 3) + j) * A.count];
+    }
+    for (int j = 0; j < 19; ++j) an[j] = 0.f;
+    rhs_vjp<float, Acc, PAIR>(V, A.F, A.G, fb, an, acc);
+    for (int j = 0; j < 19; ++j) s_tot[j][t] += an[j];
+    if (stage == 0)
+      for (int j = 0; j < 19; ++j) s_lam[j][t] += s_tot[j][t];
+  }
+  for (int j = 0; j < 19; ++j) lam[(int64_t)j * A.count + slot] = s_lam[j][t];
+}
+
 template <typename Acc, bool PAIR>
 __global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, int sgi, float* lam, const Acc a0,
                                                            const Acc a1, const Acc a2, const Acc a3) {
@@ -190,7 +232,6 @@ __global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, in
   __shared__ float s_tot[19][128];
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= A.count) return;
-  const int t = threadIdx.x;
   const Acc acc[4] = {a0, a1, a2, a3};
   const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
   MixedRay R;
@@ -200,35 +241,7 @@ __global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, in
     init_mixed(d, R, y);
   }
   mixed_observer(A.G, x0);
-  for (int j = 0; j < 19; ++j) s_lam[j][t] = lam[(int64_t)j * A.count + slot];
-  const float* tape = (const float*)A.seg;
-  const int s0 = sgi * A.C, s1 = min(s0 + A.C, A.n_steps);
-#pragma unroll 1
-  for (int st = s1 - 1; st >= s0; --st) {
-    const float* rec = tape + (int64_t)(st - s0) * kTapeStep * A.count + slot;
-    for (int j = 0; j < 19; ++j) s_tot[j][t] = 0.f;
-    float an[19];  // a of the stage after this one
-    for (int j = 0; j < 19; ++j) an[j] = 0.f;
-#pragma unroll 1
-    for (int stage = 3; stage >= 0; --stage) {
-      const float c = (stage == 0) ? 0.f : ((stage == 3) ? 1.f : 0.5f);
-      const float wl = (stage == 0 || stage == 3) ? (1.f / 6.f) : (1.f / 3.f);
-      const float wa = (stage == 3) ? 0.f : ((stage == 2) ? 1.f : 0.5f);
-      float fb[19];
-      for (int j = 0; j < 19; ++j) fb[j] = wl * s_lam[j][t] + wa * an[j];
-      StageView<float> V;
-      {
-        float u[19];
-        for (int j = 0; j < 19; ++j) u[j] = rec[(int64_t)(19 * stage + j) * A.count];
-        stage_view_mixed(u, (float)st + c, R, A.G, x0, V);
-      }
-      for (int j = 0; j < 19; ++j) an[j] = 0.f;
-      rhs_vjp<float, Acc, PAIR>(V, A.F, A.G, fb, an, acc);
-      for (int j = 0; j < 19; ++j) s_tot[j][t] += an[j];
-    }
-    for (int j = 0; j < 19; ++j) s_lam[j][t] += s_tot[j][t];
-  }
-  for (int j = 0; j < 19; ++j) lam[(int64_t)j * A.count + slot] = s_lam[j][t];
+  sweep_segment<Acc, PAIR>(A, sgi, slot, R, x0, lam, acc, s_lam, s_tot);
 }
 
 // ------------------------------------------------------------- FP64 mode

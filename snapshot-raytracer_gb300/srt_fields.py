@@ -98,7 +98,12 @@ def gaussian_fields_np(n, seed=0, phi_rms=PHI_RMS, b_rms=B_RMS):
 
 def gaussian_fields_torch(n, seed=0, phi_rms=PHI_RMS, b_rms=B_RMS, device="cuda"):
     """torch / cuFFT generator for large grids. Returns (phi, b_xyz) as float32
-    tensors on `device`, shaped (n2, n1, n0) and (n2, n1, n0, 3)."""
+    tensors on `device`, shaped (n2, n1, n0) and (n2, n1, n0, 3).
+
+    Memory-lean for 2048^3 on one GPU: the three white-noise spectra of B are
+    drawn one at a time (their generator states are kept, so each is drawn
+    again when its component is formed), and the rms normalisations are summed
+    slice by slice in float64. Peak: b, phi and three complex half-spectra."""
     import torch
 
     n0, n1, n2 = (n, n, n) if np.isscalar(n) else n
@@ -108,32 +113,51 @@ def gaussian_fields_torch(n, seed=0, phi_rms=PHI_RMS, b_rms=B_RMS, device="cuda"
     ky = (2 * np.pi * torch.fft.fftfreq(n1, device=device)).view(1, -1, 1)
     kz = (2 * np.pi * torch.fft.fftfreq(n2, device=device)).view(-1, 1, 1)
 
-    def amp_of(k2):
-        a = torch.zeros_like(k2)
-        m = (k2 > 0) & (k2 <= np.pi ** 2)
-        a[m] = k2[m] ** (-0.75)
-        return a
-
     def k2_of():
         return kx * kx + ky * ky + kz * kz
 
-    def noise():
-        return torch.randn((n2, n1, n0), generator=g, device=device, dtype=torch.float32)
+    def amp_of(k2):  # in place on k2: k^-3/2 for 0 < k <= k_Nyquist, else 0
+        m = (k2 > 0) & (k2 <= np.pi ** 2)
+        k2.masked_fill_(~m, 1.0)
+        k2.pow_(-0.75)
+        k2.mul_(m)
+        return k2
 
-    w = torch.fft.rfftn(noise())
+    def noise_spectrum():
+        return torch.fft.rfftn(torch.randn((n2, n1, n0), generator=g, device=device, dtype=torch.float32))
+
+    def rms(x):
+        acc = torch.zeros((), dtype=torch.float64, device=x.device)
+        for z in range(x.shape[0]):
+            sl = x[z].double()
+            acc += (sl * sl).sum()
+        return torch.sqrt(acc / x.numel()).float()
+
+    w = noise_spectrum()
     w *= amp_of(k2_of())
     phi = torch.fft.irfftn(w, s=(n2, n1, n0))
     del w
-    phi *= phi_rms / torch.sqrt(torch.mean(phi.double() * phi.double())).float()
+    phi *= phi_rms / rms(phi)
+    # transverse projection: B_c = (W_c - k_c (k.W) / k^2) amp
+    states, kdotw = [], None
+    for kc in (kx, ky, kz):
+        states.append(g.get_state())
+        wc = noise_spectrum()
+        wc *= kc
+        if kdotw is None:
+            kdotw = wc
+        else:
+            kdotw += wc
+            del wc
+    kdotw /= torch.where(k2_of() > 0, k2_of(), torch.ones((), device=device))
     b = torch.empty((n2, n1, n0, 3), device=device, dtype=torch.float32)
-    W = [torch.fft.rfftn(noise()) for _ in range(3)]
-    k2 = k2_of()
-    kdotw = (kx * W[0] + ky * W[1] + kz * W[2]) / torch.where(k2 > 0, k2, torch.ones_like(k2))
-    amp = amp_of(k2)
-    del k2
     for c, kc in enumerate((kx, ky, kz)):
-        b[..., c] = torch.fft.irfftn((W[c] - kc * kdotw) * amp, s=(n2, n1, n0))
-        W[c] = None
-    del kdotw, amp
-    b *= b_rms / torch.sqrt(torch.mean(b.double() * b.double())).float()
+        g.set_state(states[c])
+        wc = noise_spectrum()
+        wc.addcmul_(kdotw, kc.to(wc.dtype), value=-1)  # wc -= kc kdotw, no temporary
+        wc *= amp_of(k2_of())
+        b[..., c] = torch.fft.irfftn(wc, s=(n2, n1, n0))
+        del wc
+    del kdotw
+    b *= b_rms / rms(b)
     return phi.contiguous(), b.contiguous()
