@@ -75,6 +75,11 @@ extern "C" {
 #define SRT_MIXED_NO_REFINE 64u /* srt_forward, MIXED: keep the FP32 result of
                                    rays that passed within 1e-7 cell of a cell
                                    face instead of re-tracing them in FP64 */
+#define SRT_NESTED_RANGE 128u /* srt_forward: [pix_begin, pix_begin + pix_count)
+                                 is a range of NESTED pixel indices (nside a power
+                                 of two; base pixel b is [b nside^2, (b+1) nside^2))
+                                 and maps[m][i] belongs to NESTED pixel
+                                 pix_begin + i */
 
 #define SRT_NUM_MAPS 6
 
@@ -141,13 +146,17 @@ int64_t srt_fields_bytes(const srt_fields* fields);
  * the FP32 trajectory's error bound, 4e-7 (max|dx| + s max|dn|) + 1e-10 grid
  * units, where the FP32 and FP64 trajectories could pick different cells (the
  * Catmull-Rom Hessian jumps across faces); those rays then equal the FP64
- * result bit for bit (SRT_MIXED_NO_REFINE skips this). The CLI's batch b is pix_begin = b*nside^2,
- * pix_count = nside^2 (snapshot-raytracer.cu:708-717); all pixels is
- * pix_begin = 0, pix_count = 12*nside^2.
+ * result bit for bit (SRT_MIXED_NO_REFINE skips this). The CLI's batch b is
+ * pix_begin = b*nside^2, pix_count = nside^2 (snapshot-raytracer.cu:708-717);
+ * all pixels is pix_begin = 0, pix_count = 12*nside^2. With SRT_NESTED_RANGE
+ * the range counts NESTED pixels instead (HEALPix base pixel b, the batch the
+ * reference's README describes, is [b*nside^2, (b+1)*nside^2)), and
+ * maps[m][i] belongs to NESTED pixel pix_begin + i.
  * Replaces snapshot-raytracer.cu:857-913 (pix2ang loop, theta/phi upload,
  * raytracing_kernel launch) and the map read-back of :941-987.
  * Errors: nside < 1 or nside > 2^16, pix range outside [0, 12*nside^2],
- * n_steps < 1 or > 2^22, unknown precision -> SRT_ERR_INVALID_ARGUMENT. */
+ * n_steps < 1 or > 2^22, unknown precision, SRT_NESTED_RANGE with an nside
+ * that is not a power of two -> SRT_ERR_INVALID_ARGUMENT. */
 int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
                 int n_steps, int precision, float* const maps[SRT_NUM_MAPS], unsigned flags,
                 void* stream, srt_stats* stats);

@@ -105,8 +105,8 @@ def build(verbose=False, oracle=True, reference=True):
         _run([NVCC, *GENCODE, "-shared", "-o", LIBSRT, *objs], verbose)
         cli_src = os.path.join(CSRC, "srt_cli.cpp")
         if os.path.isfile(cli_src):
-            _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"), cli_src, "-o", CLI,
-                  "-L" + LIBDIR, "-lsrt", "-Wl,-rpath,$ORIGIN/lib"], verbose)
+            _run(["g++", "-O2", "-std=c++17", "-Wall", "-pthread", "-I" + os.path.join(ROOT, "include"), cli_src,
+                  "-o", CLI, "-L" + LIBDIR, "-lsrt", "-Wl,-rpath,$ORIGIN/lib"], verbose)
         for j in side:
             j.result()
     return LIBSRT

@@ -85,6 +85,21 @@ using namespace srt;
     }                                            \
   } while (0)
 
+namespace {
+// The upload's staging slabs, copy stream and events (each may be null).
+void release_upload(float*& slab, cudaStream_t& cs, cudaEvent_t* copied, cudaEvent_t* padded) {
+  if (slab) cudaFree(slab);
+  if (cs) cudaStreamDestroy(cs);
+  for (int i = 0; i < 2; ++i) {
+    if (copied[i]) cudaEventDestroy(copied[i]);
+    if (padded[i]) cudaEventDestroy(padded[i]);
+    copied[i] = padded[i] = nullptr;
+  }
+  slab = nullptr;
+  cs = nullptr;
+}
+}  // namespace
+
 extern "C" {
 
 int srt_abi_version(void) { return SRT_ABI_VERSION; }
@@ -119,6 +134,8 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
   const bool dev_in = (flags & SRT_INPUT_DEVICE) != 0;
   int rc = SRT_OK;
   float* slab = nullptr;
+  cudaStream_t cs = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr}, padded[2] = {nullptr, nullptr};
   srt_fields* f = new (std::nothrow) srt_fields();
   if (!f) return set_error(SRT_ERR_OUT_OF_MEMORY, "srt_fields_create: host allocation failed");
   {
@@ -137,30 +154,46 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
       for (int c = 0; c < 3; ++c)
         SRT_CUDA_TRY(launch_pad_slab(b_xyz, 3, c, f->b[c], f->n, f->pn, 0, n2, s), "pad B");
     } else {
-      // stream host planes through one device slab
+      // Stream host planes through two device slabs: the copy of chunk i + 1
+      // (on a copy stream) overlaps the pad kernel of chunk i (on s); a slab
+      // is refilled only after its pad kernel has run.
       int64_t kslab = kSlabBytes / (plane * 3 * (int64_t)sizeof(float));
       if (kslab < 1) kslab = 1;
       if (kslab > n2) kslab = n2;
-      SRT_CUDA_TRY(cudaMalloc(&slab, kslab * plane * 3 * sizeof(float)), "cudaMalloc(slab)");
-      for (int64_t k0 = 0; k0 < n2; k0 += kslab) {
-        const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
-        SRT_CUDA_TRY(cudaMemcpyAsync(slab, phi + k0 * plane, (k1 - k0) * plane * sizeof(float),
-                                     cudaMemcpyHostToDevice, s),
-                     "copy phi slab");
-        SRT_CUDA_TRY(launch_pad_slab(slab, 1, 0, f->phi, f->n, f->pn, k0, k1, s), "pad phi");
+      const int64_t slab_floats = kslab * plane * 3;
+      SRT_CUDA_TRY(cudaMalloc(&slab, 2 * slab_floats * sizeof(float)), "cudaMalloc(slabs)");
+      SRT_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
+      for (int i = 0; i < 2; ++i) {
+        SRT_CUDA_TRY(cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming), "cudaEventCreate");
+        SRT_CUDA_TRY(cudaEventCreateWithFlags(&padded[i], cudaEventDisableTiming), "cudaEventCreate");
       }
-      for (int64_t k0 = 0; k0 < n2; k0 += kslab) {
-        const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
-        SRT_CUDA_TRY(cudaMemcpyAsync(slab, b_xyz + 3 * k0 * plane, 3 * (k1 - k0) * plane * sizeof(float),
-                                     cudaMemcpyHostToDevice, s),
-                     "copy B slab");
-        for (int c = 0; c < 3; ++c)
-          SRT_CUDA_TRY(launch_pad_slab(slab, 3, c, f->b[c], f->n, f->pn, k0, k1, s), "pad B");
+      int64_t chunk = 0;
+      // pass 0: phi (one component per voxel); pass 1: B (three, interleaved)
+      for (int pass = 0; pass < 2; ++pass) {
+        const int comps = pass == 0 ? 1 : 3;
+        const float* src = pass == 0 ? phi : b_xyz;
+        for (int64_t k0 = 0; k0 < n2; k0 += kslab, ++chunk) {
+          const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
+          const int sl = (int)(chunk & 1);
+          float* buf = slab + sl * slab_floats;
+          if (chunk >= 2) SRT_CUDA_TRY(cudaStreamWaitEvent(cs, padded[sl], 0), "wait pad");
+          SRT_CUDA_TRY(cudaMemcpyAsync(buf, src + comps * k0 * plane, comps * (k1 - k0) * plane * sizeof(float),
+                                       cudaMemcpyHostToDevice, cs),
+                       "copy field slab");
+          SRT_CUDA_TRY(cudaEventRecord(copied[sl], cs), "cudaEventRecord");
+          SRT_CUDA_TRY(cudaStreamWaitEvent(s, copied[sl], 0), "wait copy");
+          if (pass == 0) {
+            SRT_CUDA_TRY(launch_pad_slab(buf, 1, 0, f->phi, f->n, f->pn, k0, k1, s), "pad phi");
+          } else {
+            for (int c = 0; c < 3; ++c)
+              SRT_CUDA_TRY(launch_pad_slab(buf, 3, c, f->b[c], f->n, f->pn, k0, k1, s), "pad B");
+          }
+          SRT_CUDA_TRY(cudaEventRecord(padded[sl], s), "cudaEventRecord");
+        }
       }
     }
     if (!(flags & SRT_ASYNC) || slab) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
-    if (slab) cudaFree(slab);
-    slab = nullptr;
+    release_upload(slab, cs, copied, padded);
     if (!(flags & SRT_FIELDS_NO_PAIRS)) {
       // row-pair arrays for the packed MIXED path, when they fit with room to spare
       const int64_t pair_bytes = 4 * f->pn[0] * (f->pn[1] - 1) * f->pn[2] * (int64_t)sizeof(float2);
@@ -179,7 +212,9 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
   *out = f;
   return SRT_OK;
 fail:
-  if (slab) cudaFree(slab);
+  if (cs) cudaStreamSynchronize(cs);
+  cudaStreamSynchronize(s);
+  release_upload(slab, cs, copied, padded);
   srt_fields_destroy(f);
   return rc;
 }
@@ -213,6 +248,10 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
   if (pix_begin < 0 || pix_count < 0 || pix_begin > npix || pix_count > npix - pix_begin)
     return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: pixel range [%lld, %lld) outside [0, %lld)",
                      (long long)pix_begin, (long long)(pix_begin + pix_count), (long long)npix);
+  const bool nested = (flags & SRT_NESTED_RANGE) != 0;
+  if (nested && (nside & (nside - 1)) != 0)
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: NESTED pixel ranges need a power-of-two nside, got %lld",
+                     (long long)nside);
   if (n_steps < 1 || n_steps > (1 << 22))
     return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: invalid n_steps %d", n_steps);
   if (precision != SRT_PRECISION_FP64 && precision != SRT_PRECISION_MIXED && precision != SRT_PRECISION_REF16)
@@ -261,9 +300,10 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     int l = 0;
     while ((int64_t(1) << l) < nside) ++l;
     a.log2p = l;
-    a.launch_rays = 12 * (int64_t(1) << (2 * l));
+    a.launch_rays = nested ? pix_count : 12 * (int64_t(1) << (2 * l));
     a.pix_begin = pix_begin;
     a.pix_count = pix_count;
+    a.nested = nested;
     a.n_steps = n_steps;
     a.refine_list = nullptr;
     a.refine_count = nullptr;

@@ -20,6 +20,16 @@
 //   --overwrite                   replace existing output files
 //   --outdir DIR                  write the maps to DIR instead of the cwd
 //   --timing                      print one JSON line with phase timings
+//   --base-pixel                  batch b is HEALPix base pixel b (the NESTED
+//                                 range [b*Nside^2, (b+1)*Nside^2), which the
+//                                 reference's README describes; Nside a power
+//                                 of two) instead of the RING range
+//   --xyz-order hdf5              x is the fastest HDF5 axis with its own
+//                                 extent (n0 = dims[2], n2 = dims[0]), which
+//                                 keeps non-cubic grids consistent; by default
+//                                 n0 = dims[0], as the reference does
+//
+// The six maps are written by six threads at once.
 //
 // Deviations, all on inputs the reference mishandles: a non-numeric Nside /
 // n_steps / batch is reported as an error instead of an uncaught exception, and
@@ -32,6 +42,7 @@
 #include <cstring>
 #include <iostream>
 #include <string>
+#include <thread>
 #include <vector>
 #include "srt.h"
 
@@ -63,7 +74,8 @@ void usage(const char* prog) {
   std::cerr << "  <Nside>: HEALPix Nside parameter for output maps" << std::endl;
   std::cerr << "  <n_steps>: Number of integration steps for raytracing (1 step = 1 grid unit)" << std::endl;
   std::cerr << "  [<batch>]: Optional batch index for processing a subset of pixels" << std::endl;
-  std::cerr << "  options: [--precision mixed|fp64|ref16] [--overwrite] [--outdir DIR] [--timing]" << std::endl;
+  std::cerr << "  options: [--precision mixed|fp64|ref16] [--overwrite] [--outdir DIR] [--timing] [--base-pixel]"
+               " [--xyz-order reference|hdf5]" << std::endl;
 }
 
 }  // namespace
@@ -71,7 +83,7 @@ void usage(const char* prog) {
 int main(int argc, char* argv[]) {
   std::vector<const char*> pos;
   int precision = SRT_PRECISION_MIXED;
-  bool overwrite = false, timing = false;
+  bool overwrite = false, timing = false, base_pixel = false, hdf5_order = false;
   std::string outdir;
   if (const char* e = getenv("SRT_PRECISION")) {
     if (!strcmp(e, "fp64")) precision = SRT_PRECISION_FP64;
@@ -93,6 +105,15 @@ int main(int argc, char* argv[]) {
       timing = true;
     } else if (!strcmp(argv[i], "--outdir") && i + 1 < argc) {
       outdir = argv[++i];
+    } else if (!strcmp(argv[i], "--base-pixel")) {
+      base_pixel = true;
+    } else if (!strcmp(argv[i], "--xyz-order") && i + 1 < argc) {
+      const char* o = argv[++i];
+      if (!strcmp(o, "hdf5")) hdf5_order = true;
+      else if (strcmp(o, "reference")) {
+        std::cerr << "Invalid xyz order: " << o << std::endl;
+        return -1;
+      }
     } else {
       pos.push_back(argv[i]);
     }
@@ -180,10 +201,19 @@ int main(int argc, char* argv[]) {
       return -1;
     }
   }
+  const bool nested = base_pixel && batch >= 0;
+  if (nested && (nside & (nside - 1)) != 0) {
+    std::cerr << "--base-pixel needs a power-of-two Nside, got " << nside << std::endl;
+    srt_free(phi);
+    srt_free(bxyz);
+    return -1;
+  }
+  // grid extents, fastest first
+  const int64_t g0 = hdf5_order ? dims[2] : dims[0], g2 = hdf5_order ? dims[0] : dims[2];
 
   std::cout << "Allocating device memory and copying data to device..." << std::endl;
   srt_fields* fields = nullptr;
-  if (srt_fields_create(phi, bxyz, dims[0], dims[1], dims[2], 0, nullptr, &fields) != SRT_OK) {
+  if (srt_fields_create(phi, bxyz, g0, dims[1], g2, 0, nullptr, &fields) != SRT_OK) {
     std::cerr << "Failed to copy data to device: " << last_error() << std::endl;
     srt_free(phi);
     srt_free(bxyz);
@@ -194,13 +224,13 @@ int main(int argc, char* argv[]) {
   const double t_up = now_ms();
 
   std::cout << "Computing theta and phi angles..." << std::endl;
-  std::vector<float> outmap((size_t)npix, 0.0f);
   std::vector<float> part((size_t)(6 * count));
   float* rows[6];
   for (int m = 0; m < 6; ++m) rows[m] = part.data() + (size_t)m * count;
   std::cout << "Launching raytracing kernel..." << std::endl;
   srt_stats st;
-  if (srt_forward(fields, nside, istart, count, n_steps, precision, rows, 0, nullptr, &st) != SRT_OK) {
+  if (srt_forward(fields, nside, istart, count, n_steps, precision, rows, nested ? SRT_NESTED_RANGE : 0u, nullptr,
+                  &st) != SRT_OK) {
     std::cerr << "Kernel execution error: " << last_error() << std::endl;
     srt_fields_destroy(fields);
     return -1;
@@ -213,13 +243,28 @@ int main(int argc, char* argv[]) {
   if (batch < 0) batch = 0;
   static const char* names[6] = {"dAmap", "ellipticity1map", "ellipticity2map", "rotationmap", "deflection1map",
                                  "deflection2map"};
+  // one full-sky RING map per thread: the batch's values at their RING
+  // index (a NESTED range is scattered through nest2ring), zero elsewhere
+  std::vector<std::string> errors(6);
+  std::vector<std::thread> writers;
   for (int m = 0; m < 6; ++m) {
-    char fname[512];
-    snprintf(fname, sizeof(fname), "%s%s%s_batch%d.fits", outdir.c_str(), outdir.empty() ? "" : "/", names[m], batch);
-    memcpy(outmap.data() + istart, rows[m], (size_t)count * sizeof(float));
-    if (srt_fits_write_map(fname, outmap.data(), nside, 0, "C", overwrite ? 1 : 0) != SRT_OK)
-      std::cerr << last_error() << std::endl;
+    writers.emplace_back([&, m]() {
+      std::vector<float> full((size_t)npix, 0.0f);
+      if (nested) {
+        for (int64_t i = 0; i < count; ++i) full[(size_t)srt_nest2ring(nside, istart + i)] = rows[m][i];
+      } else {
+        memcpy(full.data() + istart, rows[m], (size_t)count * sizeof(float));
+      }
+      char fname[512];
+      snprintf(fname, sizeof(fname), "%s%s%s_batch%d.fits", outdir.c_str(), outdir.empty() ? "" : "/", names[m],
+               batch);
+      if (srt_fits_write_map(fname, full.data(), nside, 0, "C", overwrite ? 1 : 0) != SRT_OK)
+        errors[m] = last_error();
+    });
   }
+  for (auto& w : writers) w.join();
+  for (int m = 0; m < 6; ++m)
+    if (!errors[m].empty()) std::cerr << errors[m] << std::endl;
   const double t_end = now_ms();
   std::cout << "All done!" << std::endl;
   if (timing) {

@@ -28,16 +28,17 @@ int cuda_error(cudaError_t e, const char* what);
 struct TraceArgs {
   FieldPtrs F;
   Geom G;
-  int64_t nside;
-  int log2p;           // launch order: Morton over a 2^log2p square per face
-  int64_t launch_rays; // 12 * 4^log2p
-  int64_t pix_begin, pix_count;
-  int n_steps;
-  float* maps[6];
-  // MIXED: rays that came within the cell-face guard are appended here
-  // (NULL: no fallback) and re-traced in FP64 by launch_refine.
-  int64_t* refine_list;
-  unsigned long long* refine_count;
+  int64_t nside = 0;
+  int log2p = 0;            // launch order: Morton over a 2^log2p square per face
+  int64_t launch_rays = 0;  // launch slots: 12 * 4^log2p (RING ranges) or pix_count (NESTED)
+  int64_t pix_begin = 0, pix_count = 0;
+  bool nested = false;      // [pix_begin, pix_begin + pix_count) is a NESTED range
+  int n_steps = 0;
+  float* maps[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // MIXED: the output slots of rays that came within the cell-face guard are
+  // appended here (NULL: no fallback) and re-traced in FP64 by launch_refine.
+  int64_t* refine_list = nullptr;
+  unsigned long long* refine_count = nullptr;
 };
 
 Geom make_geom(const srt_fields* f);

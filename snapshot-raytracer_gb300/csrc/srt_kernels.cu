@@ -95,15 +95,17 @@ cudaError_t launch_pair_build(const float* src, float2* dst, const int64_t pn[3]
 template <int MODE>
 __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ? SRT_MIXED_MIN_BLOCKS : 1)
     trace_kernel(const TraceArgs A) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= A.launch_rays) return;
-  // launch order: face-major, Morton (NESTED for power-of-two nside) in-face
+  const int64_t tl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= A.launch_rays) return;
+  // launch order: face-major, Morton (NESTED for power-of-two nside) in-face;
+  // a NESTED range launches its own slots
+  const int64_t t = A.nested ? A.pix_begin + tl : tl;
   const int64_t face = t >> (2 * A.log2p);
   int64_t ix, iy;
   hp_deinterleave(t & ((int64_t(1) << (2 * A.log2p)) - 1), &ix, &iy);
   if (ix >= A.nside || iy >= A.nside) return;
   const int64_t ring = hp_xyf2ring(A.nside, ix, iy, (int)face);
-  const int64_t o = ring - A.pix_begin;
+  const int64_t o = A.nested ? tl : ring - A.pix_begin;
   if (o < 0 || o >= A.pix_count) return;
   const RayDir d = ray_dir_pix(A.nside, ring);
   float out[6];
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ?
     const bool near = trace_ray_mixed<MODE == kMIXED_PAIR>(A.F, A.G, d, A.n_steps, out, guard_m[threadIdx.x]);
     if (near && A.refine_list) {
       const unsigned long long k = atomicAdd(A.refine_count, 1ull);
-      if (k < (unsigned long long)A.pix_count) A.refine_list[k] = o + A.pix_begin;
+      if (k < (unsigned long long)A.pix_count) A.refine_list[k] = o;
     }
   } else {
     trace_ray_std<MODE == kREF16 ? kREF16 : kFP64>(A.F, A.G, d, A.n_steps, out);
@@ -197,7 +199,8 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A) {
   for (int64_t k0 = (int64_t)blockIdx.x * kRays; k0 < n; k0 += (int64_t)gridDim.x * kRays) {
     const int64_t k = k0 + lane / LANES;
     if (k >= n) continue;
-    const int64_t ring = A.refine_list[k];
+    const int64_t o = A.refine_list[k];  // output slot
+    const int64_t ring = A.nested ? hp_nest2ring(A.nside, A.pix_begin + o) : A.pix_begin + o;
     const RayDir d = ray_dir_pix(A.nside, ring);
     double y[19];
     init_std(d, A.G, y);
@@ -215,7 +218,7 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A) {
       float out[6];
       extract_std(d, A.G, y, out);
 #pragma unroll
-      for (int m = 0; m < 6; ++m) A.maps[m][ring - A.pix_begin] = out[m];
+      for (int m = 0; m < 6; ++m) A.maps[m][o] = out[m];
     }
   }
 }

@@ -27,6 +27,7 @@ SRT_ACCUMULATE = 8
 SRT_DETERMINISTIC = 16
 SRT_FIELDS_NO_PAIRS = 32
 SRT_MIXED_NO_REFINE = 64
+SRT_NESTED_RANGE = 128
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
           -5: "format error", -6: "no CUDA device", -7: "unsupported"}
@@ -196,8 +197,9 @@ class Fields:
         self.close()
 
     def forward(self, nside, n_steps, pix_begin=0, pix_count=None, precision="mixed", out=None, stream=None,
-                async_=False, refine=True):
-        """Six maps of RING pixels [pix_begin, pix_begin + pix_count).
+                async_=False, refine=True, nested=False):
+        """Six maps of RING pixels [pix_begin, pix_begin + pix_count) (NESTED
+        pixels when nested=True; base pixel b is [b nside^2, (b+1) nside^2)).
         out: None (returns a new (6, count) float32 numpy array), a (6, count)
         numpy array, or a (6, count) CUDA tensor (device output). Returns
         (maps, Stats)."""
@@ -212,7 +214,7 @@ class Fields:
         rows = _FP6(*[p + m * pix_count * 4 for m in range(6)])
         st = Stats()
         flags = (SRT_OUTPUT_DEVICE if dev else 0) | (SRT_ASYNC if async_ else 0) | \
-            (0 if refine else SRT_MIXED_NO_REFINE)
+            (0 if refine else SRT_MIXED_NO_REFINE) | (SRT_NESTED_RANGE if nested else 0)
         _check(lib().srt_forward(self._h, nside, pix_begin, pix_count, n_steps, PRECISION[precision], rows, flags,
                                  _stream_ptr(stream), ctypes.byref(st)))
         return out, st

@@ -102,8 +102,9 @@ def gaussian_fields_torch(n, seed=0, phi_rms=PHI_RMS, b_rms=B_RMS, device="cuda"
 
     Memory-lean for 2048^3 on one GPU: the three white-noise spectra of B are
     drawn one at a time (their generator states are kept, so each is drawn
-    again when its component is formed), and the rms normalisations are summed
-    slice by slice in float64. Peak: b, phi and three complex half-spectra."""
+    again when its component is formed), the rms normalisations are summed
+    slice by slice in float64, and above 2^32 voxels phi is parked in host
+    memory while B is formed. Peak: b and three complex half-spectra."""
     import torch
 
     n0, n1, n2 = (n, n, n) if np.isscalar(n) else n
@@ -138,6 +139,12 @@ def gaussian_fields_torch(n, seed=0, phi_rms=PHI_RMS, b_rms=B_RMS, device="cuda"
     phi = torch.fft.irfftn(w, s=(n2, n1, n0))
     del w
     phi *= phi_rms / rms(phi)
+    # above 2^32 voxels (2048^3: 32 GiB a field) phi waits in host memory while
+    # B is formed, so that B's spectra and cuFFT's workspace fit beside b
+    park = n0 * n1 * n2 > (1 << 32) and phi.is_cuda
+    if park:
+        phi = phi.cpu()
+        torch.cuda.empty_cache()
     # transverse projection: B_c = (W_c - k_c (k.W) / k^2) amp
     states, kdotw = [], None
     for kc in (kx, ky, kz):
@@ -160,4 +167,7 @@ def gaussian_fields_torch(n, seed=0, phi_rms=PHI_RMS, b_rms=B_RMS, device="cuda"
         del wc
     del kdotw
     b *= b_rms / rms(b)
+    if park:
+        torch.cuda.empty_cache()
+        phi = phi.to(device)
     return phi.contiguous(), b.contiguous()

@@ -73,3 +73,39 @@ def test_cli_keeps_existing_outputs(srt, tmp_path):
     r = subprocess.run([CLI, pp, pb, "2", "4", "--overwrite"], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 0
     assert srt.fits_read_map(str(tmp_path / "dAmap_batch0.fits"))[1] == 2
+
+
+def test_cli_base_pixel_batch(srt, tmp_path):
+    """--base-pixel: batch b is HEALPix base pixel b (NESTED range), the maps
+    are zero outside it and equal the full-sky maps inside it."""
+    phi, b = srt_fields.gaussian_fields_np(32, seed=6)
+    pp, pb = write_inputs(srt, tmp_path, phi, b)
+    nside, steps, face = 8, 16, 7
+    r = subprocess.run([CLI, pp, pb, str(nside), str(steps), str(face), "--base-pixel"], capture_output=True,
+                       text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    full = srt.trace(phi, b, nside, steps, precision="mixed")
+    inside = np.zeros(12 * nside * nside, bool)
+    inside[[srt.nest2ring(nside, face * nside * nside + i) for i in range(nside * nside)]] = True
+    for m, name in enumerate(NAMES):
+        got, ns, nest = srt.fits_read_map(str(tmp_path / ("%s_batch%d.fits" % (name, face))))
+        assert ns == nside and not nest
+        assert not np.any(got[~inside])
+        assert np.array_equal(got[inside].view(np.uint32), full[m][inside].view(np.uint32)), name
+    r = subprocess.run([CLI, pp, pb, "6", "4", "1", "--base-pixel"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 255 and "power-of-two" in r.stderr
+
+
+def test_cli_hdf5_axis_order_noncubic(srt, tmp_path):
+    """--xyz-order hdf5: x is the fastest HDF5 axis with its own extent, so a
+    non-cubic grid gives the library's maps for the same array."""
+    phi, b = srt_fields.gaussian_fields_np((24, 16, 20), seed=9)  # numpy shape (20, 16, 24): x extent 24
+    pp, pb = write_inputs(srt, tmp_path, phi, b)
+    nside, steps = 4, 12
+    r = subprocess.run([CLI, pp, pb, str(nside), str(steps), "--xyz-order", "hdf5"], capture_output=True, text=True,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    ref = srt.trace(phi, b, nside, steps, precision="mixed")
+    for m, name in enumerate(NAMES):
+        got = srt.fits_read_map(str(tmp_path / ("%s_batch0.fits" % name)))[0]
+        assert np.array_equal(got.view(np.uint32), ref[m].view(np.uint32)), name

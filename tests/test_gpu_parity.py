@@ -201,3 +201,20 @@ def test_mixed_refines_face_crossing_rays(srt, orc):
     # different sides (unrefined dA error 5e-3 of the map's rms): refined, the
     # MIXED maps meet the FP32 tolerance
     _assert_close(mr, m64, "mixed", "refined mixed vs fp64")
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_nested_range_matches_ring(srt, precision):
+    """SRT_NESTED_RANGE: a NESTED pixel range (here base pixel 5 and a part of
+    base pixel 0) gives, pixel for pixel, the maps of the RING full sky."""
+    phi, b = srt_fields.gaussian_fields_np(32, seed=12)
+    nside, steps = 8, 20
+    with srt.Fields(phi, b) as f:
+        full, _ = f.forward(nside, steps, precision=precision)
+        for begin, count in ((5 * nside * nside, nside * nside), (3, 29)):
+            got, st = f.forward(nside, steps, begin, count, precision=precision, nested=True)
+            assert st.rays == count
+            ring = [srt.nest2ring(nside, begin + i) for i in range(count)]
+            assert np.array_equal(got.view(np.uint32), full[:, ring].view(np.uint32))
+        with pytest.raises(srt.SrtError):
+            f.forward(6, steps, 0, 36, precision=precision, nested=True)
