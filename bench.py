@@ -253,6 +253,20 @@ def run_adjoint_leg(spec, seed, dev):
         res["vjp_over_forward"] = res["vjp_ms"] / res["forward_ms"]
         res["vjp_over_fp32_forward"] = res["vjp_ms"] / res["forward_fp32_only_ms"]
         res["vjp_ray_steps_per_s"] = npix * S / (res["vjp_ms"] * 1e-3)
+        # the forward/vjp pair: a forward that keeps its checkpoints, then the
+        # backward sweep alone
+        ftape, btape = [], []
+        for i in range(reps):
+            _, tape, stf = f.forward_tape(nside, S, ckpt_every=C, out=out, stream=stream)
+            _, _, stb = tape.vjp(w, dphi=gphi, db_xyz=gb, stream=stream, wrt=wrt)
+            tape.close()
+            if i > 0:
+                ftape.append(stf.trace_ms)
+                btape.append(stb.trace_ms)
+        res["forward_tape_ms"] = float(np.median(ftape))
+        res["vjp_tape_ms"] = float(np.median(btape))
+        res["vjp_tape_over_forward"] = res["vjp_tape_ms"] / res["forward_ms"]
+        res["vjp_tape_over_fp32_forward"] = res["vjp_tape_ms"] / res["forward_fp32_only_ms"]
         if n > 256 or "b" not in wrt:
             torch.cuda.synchronize()
             del phi, b, gphi, gb, out, w

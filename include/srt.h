@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SRT_ABI_VERSION 2
+#define SRT_ABI_VERSION 3
 
 /* status codes */
 #define SRT_OK 0
@@ -193,6 +193,34 @@ int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int64_t pix_beg
 int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
             int n_steps, int precision, const float* const weights[SRT_NUM_MAPS], float* dphi,
             float* db_xyz, int ckpt_every, unsigned flags, void* stream, srt_stats* stats);
+
+/* A forward trace's checkpoints, for srt_vjp_tape. */
+typedef struct srt_tape srt_tape;
+
+/* srt_forward (MIXED) that also keeps, on the device, the state of every ray
+ * every ckpt_every steps (<= 0 picks ~sqrt(n_steps)), so that srt_vjp_tape can
+ * form the gradient without tracing the rays forward again: the forward half
+ * of a forward/vjp pair. The maps are srt_forward's (flagged rays re-traced
+ * in FP64). The tape holds (n_steps/ckpt_every + 1) x 38 floats and one
+ * index per ray; the fields must outlive it. pix_count >= 1; flags:
+ * SRT_OUTPUT_DEVICE. No counterpart in the reference (it has no
+ * derivatives). */
+int srt_forward_tape(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
+                     int n_steps, int ckpt_every, float* const maps[SRT_NUM_MAPS], unsigned flags,
+                     void* stream, srt_stats* stats, srt_tape** tape);
+
+/* srt_vjp (MIXED) of the tape's forward: the same gradient as srt_vjp with the
+ * tape's arguments and checkpoint interval, without its checkpointing forward
+ * pass. flags: SRT_OUTPUT_DEVICE, SRT_ACCUMULATE, SRT_DETERMINISTIC. The tape
+ * can be swept any number of times (e.g. for several weight sets). */
+int srt_vjp_tape(const srt_tape* tape, const float* const weights[SRT_NUM_MAPS], float* dphi,
+                 float* db_xyz, unsigned flags, void* stream, srt_stats* stats);
+
+/* Device bytes held by a tape. */
+int64_t srt_tape_bytes(const srt_tape* tape);
+
+/* Release a tape (NULL is a no-op). */
+int srt_tape_destroy(srt_tape* tape);
 
 /* ---------------------------------------------------------- measurement */
 

@@ -79,6 +79,11 @@ struct AdjArgs {
   void* ckpt;         // [nseg + 1][state][count]
   void* seg;          // [C][state + 57][count]
   void* acc[4];       // padded gradient accumulators B_x, B_y, B_z, phi (NULL: not wanted)
+  // forward with a tape (srt_forward_tape): the maps, indexed by ring - pix_begin,
+  // and the output slots of rays that came within the cell-face guard
+  float* maps[6];
+  int64_t* refine_list;
+  unsigned long long* refine_count;
 };
 
 template <typename T>
@@ -97,25 +102,50 @@ __device__ __forceinline__ void load_vec(const T* base, int64_t count, int64_t s
 constexpr int kTapeStep = 4 * 19;
 
 // PAIR: the forward steps read the row-pair field arrays (srt_fields.pr).
-template <bool PAIR>
-__global__ void __launch_bounds__(128) ckpt_kernel_mixed(const AdjArgs A) {
+// Forward trace storing the state every C steps (and the final state). MAPS
+// (srt_forward_tape): also the maps, with the cell-face guard of the trace
+// kernel and its list of rays to re-trace; the arithmetic is the trace
+// kernel's, so the maps are srt_forward's.
+template <bool PAIR, bool MAPS>
+__global__ void __launch_bounds__(128, MAPS ? 2 : 1) ckpt_kernel_mixed(const AdjArgs A) {
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= A.count) return;
-  const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
+  const int64_t ring = A.rays[slot];
+  const RayDir d = ray_dir_pix(A.nside, ring);
   MixedRay R;
   float y[kMixedState], x0[3];
   mixed_observer(A.G, x0);
   init_mixed(d, R, y);
   float* ck = (float*)A.ckpt;
   store_vec(ck, A.count, slot, y, kMixedState);
+  // MAPS: the guard of the trace kernel; else disabled (cell-face proximity
+  // matters for the maps, not for the gradient)
+  __shared__ float guard_m[MAPS ? 128 : 1][3];
+  Guard gd;
+  if (MAPS) {
+    gd.m = guard_m[threadIdx.x];
+    gd.m[0] = gd.m[1] = 0.f;
+  }
 #pragma unroll 1
   for (int st = 0; st < A.n_steps; ++st) {
-    Guard gd;  // disabled: cell-face proximity matters for the maps, not for the gradient
+    if (MAPS) gd.begin_step(y);
     step_mixed<PAIR>(R, A.F, A.G, x0, st, y, nullptr, 0, gd);
+    if (MAPS) gd.end_step(st);
     const int done = st + 1;
     if (done % A.C == 0 || done == A.n_steps) {
       const int k = (done + A.C - 1) / A.C;
       store_vec(ck + (int64_t)k * kMixedState * A.count, A.count, slot, y, kMixedState);
+    }
+  }
+  if (MAPS) {
+    const int64_t o = ring - A.pix_begin;
+    float out[6];
+    extract_mixed(R, A.n_steps, y, out);
+#pragma unroll
+    for (int m = 0; m < 6; ++m) A.maps[m][o] = out[m];
+    if (gd.near && A.refine_list) {
+      const unsigned long long k = atomicAdd(A.refine_count, 1ull);
+      if (k < (unsigned long long)A.count) A.refine_list[k] = o;
     }
   }
 }
@@ -439,9 +469,79 @@ void make_acc(Acc* acc, void* const* bufs) {
     }                                \
   } while (0)
 
+namespace {
+
+// Morton-ordered list of the RING pixels in [pix_begin, pix_begin + pix_count)
+// (the forward's launch order) -> rays.
+int build_ray_list(int64_t nside, int64_t pix_begin, int64_t pix_count, cudaStream_t s, DevBuf& counts,
+                   DevBuf& offsets, DevBuf& rays, int64_t* kernels, const char* who) {
+  int rc = SRT_OK;
+  RangeArgs ra;
+  ra.nside = nside;
+  int l = 0;
+  while ((int64_t(1) << l) < nside) ++l;
+  ra.log2p = l;
+  ra.launch_rays = 12 * (int64_t(1) << (2 * l));
+  ra.pix_begin = pix_begin;
+  ra.pix_count = pix_count;
+  const int64_t nblk = (ra.launch_rays + kListBlock - 1) / kListBlock;
+  std::vector<int> hc(nblk);
+  std::vector<int64_t> ho(nblk);
+  int64_t run = 0;
+  VJP_TRY(counts.alloc(nblk * sizeof(int)), "cudaMalloc(ray counts)");
+  VJP_TRY(offsets.alloc(nblk * sizeof(int64_t)), "cudaMalloc(ray offsets)");
+  VJP_TRY(rays.alloc(pix_count * sizeof(int64_t)), "cudaMalloc(ray list)");
+  ray_count_kernel<<<(unsigned)nblk, kListBlock, 0, s>>>(ra, (int*)counts.p);
+  ++*kernels;
+  VJP_TRY(cudaGetLastError(), "ray_count_kernel");
+  VJP_TRY(cudaMemcpyAsync(hc.data(), counts.p, nblk * sizeof(int), cudaMemcpyDeviceToHost, s), "copy counts");
+  VJP_TRY(cudaStreamSynchronize(s), "ray count");
+  for (int64_t b = 0; b < nblk; ++b) {
+    ho[b] = run;
+    run += hc[b];
+  }
+  if (run != pix_count)
+    return set_error(SRT_ERR_CUDA, "%s: ray list has %lld rays, expected %lld", who, (long long)run,
+                     (long long)pix_count);
+  VJP_TRY(cudaMemcpyAsync(offsets.p, ho.data(), nblk * sizeof(int64_t), cudaMemcpyHostToDevice, s), "copy offsets");
+  ray_write_kernel<<<(unsigned)nblk, kListBlock, 0, s>>>(ra, (const int64_t*)offsets.p, (int64_t*)rays.p);
+  ++*kernels;
+  VJP_TRY(cudaGetLastError(), "ray_write_kernel");
+  // the host vectors must outlive the asynchronous copy of the offsets
+  VJP_TRY(cudaStreamSynchronize(s), "ray list");
+done:
+  return rc;
+}
+
+}  // namespace
+
+// A forward trace's checkpoints (srt_forward_tape) for srt_vjp_tape.
+struct srt_tape {
+  const srt_fields* fields = nullptr;
+  int device = 0;
+  int64_t nside = 0, pix_begin = 0, pix_count = 0;
+  int n_steps = 0, C = 0, nseg = 0;
+  int64_t* rays = nullptr;  // Morton-ordered RING pixels (device)
+  float* ckpt = nullptr;    // [nseg + 1][kMixedState][pix_count] (device)
+  int64_t bytes = 0;
+};
+
+static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
+                    int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz,
+                    int ckpt_every, unsigned flags, void* stream, srt_stats* stats, const srt_tape* tape);
+
 extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
                        int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz,
                        int ckpt_every, unsigned flags, void* stream, srt_stats* stats) {
+  return vjp_impl(fields, nside, pix_begin, pix_count, n_steps, precision, weights, dphi, db_xyz, ckpt_every, flags,
+                  stream, stats, nullptr);
+}
+
+// srt_vjp; with a tape, the rays and checkpoints of srt_forward_tape replace
+// the ray list and the checkpointing forward pass (MIXED only).
+static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
+                    int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz,
+                    int ckpt_every, unsigned flags, void* stream, srt_stats* stats, const srt_tape* tape) {
   const auto t_wall = std::chrono::steady_clock::now();
   if (!fields) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp: fields is NULL");
   if (nside < 1 || nside > (int64_t(1) << 16))
@@ -467,6 +567,7 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
   cudaStream_t s = (cudaStream_t)stream;
   int C = ckpt_every > 0 ? ckpt_every : (int)std::max(1.0, std::floor(std::sqrt((double)n_steps) + 0.5));
   if (C > n_steps) C = n_steps;
+  if (tape) C = tape->C;
   const int nseg = (n_steps + C - 1) / C;
   int rc = SRT_OK;
   int prev = 0;
@@ -498,40 +599,13 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
     float* out_phi = dev_io ? dphi : (float*)gout_phi.p;
     float* out_b = dev_io ? db_xyz : (float*)gout_b.p;
     if (pix_count > 0 && (dphi || db_xyz)) {
-      // ---- ray list
-      RangeArgs ra;
-      ra.nside = nside;
-      int l = 0;
-      while ((int64_t(1) << l) < nside) ++l;
-      ra.log2p = l;
-      ra.launch_rays = 12 * (int64_t(1) << (2 * l));
-      ra.pix_begin = pix_begin;
-      ra.pix_count = pix_count;
-      const int64_t nblk = (ra.launch_rays + kListBlock - 1) / kListBlock;
-      VJP_TRY(counts.alloc(nblk * sizeof(int)), "cudaMalloc(ray counts)");
-      VJP_TRY(offsets.alloc(nblk * sizeof(int64_t)), "cudaMalloc(ray offsets)");
-      VJP_TRY(rays.alloc(pix_count * sizeof(int64_t)), "cudaMalloc(ray list)");
-      ray_count_kernel<<<(unsigned)nblk, kListBlock, 0, s>>>(ra, (int*)counts.p);
-      ++kernels;
-      VJP_TRY(cudaGetLastError(), "ray_count_kernel");
-      std::vector<int> hc(nblk);
-      std::vector<int64_t> ho(nblk);
-      VJP_TRY(cudaMemcpyAsync(hc.data(), counts.p, nblk * sizeof(int), cudaMemcpyDeviceToHost, s), "copy counts");
-      VJP_TRY(cudaStreamSynchronize(s), "ray count");
-      int64_t run = 0;
-      for (int64_t b = 0; b < nblk; ++b) {
-        ho[b] = run;
-        run += hc[b];
+      // ---- ray list (a tape brings its own)
+      const int64_t* ray_list = tape ? tape->rays : nullptr;
+      if (!tape) {
+        rc = build_ray_list(nside, pix_begin, pix_count, s, counts, offsets, rays, &kernels, "srt_vjp");
+        if (rc != SRT_OK) goto done;
+        ray_list = (const int64_t*)rays.p;
       }
-      if (run != pix_count) {
-        rc = set_error(SRT_ERR_CUDA, "srt_vjp: ray list has %lld rays, expected %lld", (long long)run,
-                       (long long)pix_count);
-        goto done;
-      }
-      VJP_TRY(cudaMemcpyAsync(offsets.p, ho.data(), nblk * sizeof(int64_t), cudaMemcpyHostToDevice, s), "copy offsets");
-      ray_write_kernel<<<(unsigned)nblk, kListBlock, 0, s>>>(ra, (const int64_t*)offsets.p, (int64_t*)rays.p);
-      ++kernels;
-      VJP_TRY(cudaGetLastError(), "ray_write_kernel");
 
       // ---- weights on the device
       const float* wd[6];
@@ -551,7 +625,7 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
       // ---- scratch: checkpoints, segment records, padded accumulators
       const int state = fp64 ? 19 : kMixedState;
       const size_t esz = fp64 ? sizeof(double) : sizeof(float);
-      VJP_TRY(ckpt.alloc((size_t)(nseg + 1) * state * pix_count * esz), "cudaMalloc(checkpoints)");
+      if (!tape) VJP_TRY(ckpt.alloc((size_t)(nseg + 1) * state * pix_count * esz), "cudaMalloc(checkpoints)");
       // per-step records of one segment: FP64 y, k1, k2, k3; MIXED the four stage inputs
       VJP_TRY(seg.alloc((size_t)C * (fp64 ? state + 57 : kTapeStep) * pix_count * esz), "cudaMalloc(segment records)");
       if (!fp64) VJP_TRY(lam.alloc((size_t)19 * pix_count * sizeof(float)), "cudaMalloc(state cotangents)");
@@ -568,14 +642,17 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
       A.nside = nside;
       A.pix_begin = pix_begin;
       A.count = pix_count;
-      A.rays = (const int64_t*)rays.p;
+      A.rays = ray_list;
       A.n_steps = n_steps;
       A.C = C;
       A.nseg = nseg;
       for (int m = 0; m < 6; ++m) A.w[m] = wd[m];
-      A.ckpt = ckpt.p;
+      A.ckpt = tape ? (void*)tape->ckpt : ckpt.p;
       A.seg = seg.p;
       for (int fld = 0; fld < 4; ++fld) A.acc[fld] = gacc[fld].p;
+      for (int m = 0; m < 6; ++m) A.maps[m] = nullptr;
+      A.refine_list = nullptr;
+      A.refine_count = nullptr;
 
       VJP_TRY(cudaEventCreate(&e0), "cudaEventCreate");
       VJP_TRY(cudaEventCreate(&e1), "cudaEventCreate");
@@ -596,12 +673,15 @@ extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begi
         // forward with checkpoints; then per segment, backwards: recompute
         // the segment's tape, sweep it
         const bool pair = f->pr[0] != nullptr;
-        if (pair)
-          ckpt_kernel_mixed<true><<<blocks, 128, 0, s>>>(A);
-        else
-          ckpt_kernel_mixed<false><<<blocks, 128, 0, s>>>(A);
+        if (tape) {
+          // the checkpoints come from srt_forward_tape
+        } else if (pair) {
+          ckpt_kernel_mixed<true, false><<<blocks, 128, 0, s>>>(A);
+        } else {
+          ckpt_kernel_mixed<false, false><<<blocks, 128, 0, s>>>(A);
+        }
         final_cotangent_kernel_mixed<<<blocks, 128, 0, s>>>(A, (float*)lam.p);
-        kernels += 2;
+        kernels += tape ? 1 : 2;
         AccF32 af[4];
         AccFixed ax[4];
         make_acc<AccF32, float4>(af, A.acc);
@@ -678,4 +758,158 @@ done:
   if (stats)
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall).count();
   return rc;
+}
+
+// ------------------------------------------------------------------ tape
+
+extern "C" int srt_forward_tape(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
+                                int n_steps, int ckpt_every, float* const maps[SRT_NUM_MAPS], unsigned flags,
+                                void* stream, srt_stats* stats, srt_tape** out) {
+  const auto t_wall = std::chrono::steady_clock::now();
+  if (!out) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: out is NULL");
+  *out = nullptr;
+  if (!fields) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: fields is NULL");
+  if (nside < 1 || nside > (int64_t(1) << 16))
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: invalid nside %lld", (long long)nside);
+  const int64_t npix = 12 * nside * nside;
+  if (pix_begin < 0 || pix_count < 1 || pix_begin > npix || pix_count > npix - pix_begin)
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: pixel range outside [0, %lld) or empty",
+                     (long long)npix);
+  if (n_steps < 1 || n_steps > (1 << 22))
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: invalid n_steps %d", n_steps);
+  if (!maps) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: maps is NULL");
+  for (int m = 0; m < 6; ++m)
+    if (!maps[m]) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: maps[%d] is NULL", m);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  const srt_fields* f = fields;
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool dev_out = (flags & SRT_OUTPUT_DEVICE) != 0;
+  int C = ckpt_every > 0 ? ckpt_every : (int)std::max(1.0, std::floor(std::sqrt((double)n_steps) + 0.5));
+  if (C > n_steps) C = n_steps;
+  const int nseg = (n_steps + C - 1) / C;
+  int rc = SRT_OK;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (prev != f->device) cudaSetDevice(f->device);
+  srt_tape* t = new (std::nothrow) srt_tape();
+  DevBuf counts, offsets, rays, ckpt, dmaps, rlist, rcount;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int64_t kernels = 0;
+  if (!t) {
+    rc = set_error(SRT_ERR_OUT_OF_MEMORY, "srt_forward_tape: host allocation failed");
+    goto done;
+  }
+  {
+    rc = build_ray_list(nside, pix_begin, pix_count, s, counts, offsets, rays, &kernels, "srt_forward_tape");
+    if (rc != SRT_OK) goto done;
+    VJP_TRY(ckpt.alloc((size_t)(nseg + 1) * kMixedState * pix_count * sizeof(float)), "cudaMalloc(checkpoints)");
+    VJP_TRY(rlist.alloc(pix_count * sizeof(int64_t)), "cudaMalloc(refine list)");
+    VJP_TRY(rcount.alloc(sizeof(unsigned long long)), "cudaMalloc(refine count)");
+    VJP_TRY(cudaMemsetAsync(rcount.p, 0, sizeof(unsigned long long), s), "clear refine count");
+    float* dm[6];
+    if (dev_out) {
+      for (int m = 0; m < 6; ++m) dm[m] = maps[m];
+    } else {
+      VJP_TRY(dmaps.alloc(6 * pix_count * sizeof(float)), "cudaMalloc(maps)");
+      for (int m = 0; m < 6; ++m) dm[m] = (float*)dmaps.p + m * pix_count;
+    }
+    AdjArgs A;
+    memset(&A, 0, sizeof(A));
+    A.F = make_ptrs(f);
+    A.G = make_geom(f);
+    A.nside = nside;
+    A.pix_begin = pix_begin;
+    A.count = pix_count;
+    A.rays = (const int64_t*)rays.p;
+    A.n_steps = n_steps;
+    A.C = C;
+    A.nseg = nseg;
+    A.ckpt = ckpt.p;
+    for (int m = 0; m < 6; ++m) A.maps[m] = dm[m];
+    A.refine_list = (int64_t*)rlist.p;
+    A.refine_count = (unsigned long long*)rcount.p;
+    VJP_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+    VJP_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+    VJP_TRY(cudaEventRecord(e0, s), "cudaEventRecord");
+    const unsigned blocks = (unsigned)((pix_count + 127) / 128);
+    if (f->pr[0])
+      ckpt_kernel_mixed<true, true><<<blocks, 128, 0, s>>>(A);
+    else
+      ckpt_kernel_mixed<false, true><<<blocks, 128, 0, s>>>(A);
+    ++kernels;
+    VJP_TRY(cudaGetLastError(), "checkpointing forward");
+    TraceArgs ta;
+    ta.F = A.F;
+    ta.G = A.G;
+    ta.nside = nside;
+    ta.pix_begin = pix_begin;
+    ta.pix_count = pix_count;
+    ta.n_steps = n_steps;
+    for (int m = 0; m < 6; ++m) ta.maps[m] = dm[m];
+    ta.refine_list = A.refine_list;
+    ta.refine_count = A.refine_count;
+    VJP_TRY(launch_refine(ta, s, &kernels), "refine kernel launch");
+    VJP_TRY(cudaEventRecord(e1, s), "cudaEventRecord");
+    if (!dev_out)
+      for (int m = 0; m < 6; ++m)
+        VJP_TRY(cudaMemcpyAsync(maps[m], dm[m], pix_count * sizeof(float), cudaMemcpyDeviceToHost, s),
+                "copy maps to host");
+    VJP_TRY(cudaStreamSynchronize(s), "srt_forward_tape");
+    if (stats) {
+      float ms = -1.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      stats->trace_ms = ms;
+      stats->rays = pix_count;
+      stats->ray_steps = pix_count * (int64_t)n_steps;
+      stats->kernels = kernels;
+      stats->d2h_bytes = dev_out ? 0 : 6 * pix_count * (int64_t)sizeof(float);
+      unsigned long long cnt = 0;
+      if (cudaMemcpy(&cnt, rcount.p, sizeof(cnt), cudaMemcpyDeviceToHost) == cudaSuccess)
+        stats->refined_rays = (int64_t)cnt;
+    }
+    t->fields = f;
+    t->device = f->device;
+    t->nside = nside;
+    t->pix_begin = pix_begin;
+    t->pix_count = pix_count;
+    t->n_steps = n_steps;
+    t->C = C;
+    t->nseg = nseg;
+    t->rays = (int64_t*)rays.p;
+    t->ckpt = (float*)ckpt.p;
+    t->bytes = pix_count * (int64_t)sizeof(int64_t) + (int64_t)(nseg + 1) * kMixedState * pix_count * 4;
+    rays.p = nullptr;  // owned by the tape from here on
+    ckpt.p = nullptr;
+    *out = t;
+    t = nullptr;
+  }
+done:
+  delete t;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (prev != f->device) cudaSetDevice(prev);
+  if (stats)
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_wall).count();
+  return rc;
+}
+
+extern "C" int srt_vjp_tape(const srt_tape* tape, const float* const weights[SRT_NUM_MAPS], float* dphi,
+                            float* db_xyz, unsigned flags, void* stream, srt_stats* stats) {
+  if (!tape) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp_tape: tape is NULL");
+  return vjp_impl(tape->fields, tape->nside, tape->pix_begin, tape->pix_count, tape->n_steps, SRT_PRECISION_MIXED,
+                  weights, dphi, db_xyz, tape->C, flags, stream, stats, tape);
+}
+
+extern "C" int64_t srt_tape_bytes(const srt_tape* tape) { return tape ? tape->bytes : 0; }
+
+extern "C" int srt_tape_destroy(srt_tape* tape) {
+  if (!tape) return SRT_OK;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (prev != tape->device) cudaSetDevice(tape->device);
+  if (tape->rays) cudaFree(tape->rays);
+  if (tape->ckpt) cudaFree(tape->ckpt);
+  if (prev != tape->device) cudaSetDevice(prev);
+  delete tape;
+  return SRT_OK;
 }

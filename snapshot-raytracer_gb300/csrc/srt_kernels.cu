@@ -11,6 +11,7 @@
 //   * fma_probe_kernel     FP32 / FP64 FMA issue-rate probe used for the roofline
 #include <cstdio>
 #include <algorithm>
+#include <cstdlib>
 #include "srt_internal.h"
 
 namespace srt {
@@ -123,21 +124,20 @@ __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ?
   for (int m = 0; m < 6; ++m) A.maps[m][o] = out[m];
 }
 
-// FP64 re-trace of listed rays (MIXED rays near a cell face); the list's
-// length is read on the device, so no host round trip is needed.
+// Re-trace of listed rays (MIXED rays near a cell face) in FP64 arithmetic;
+// the list's length is read on the device, so no host round trip is needed.
 //
-// The rays are few (~0.1% of a sky) and FP64 runs at 1/64 of the FP32 rate.
-// A warp of 32 single-thread rays needs ~0.17 s for 512 steps however few of
-// its lanes are busy, and one such warp per SM sub-partition (608 on GB300)
-// already holds ~19k rays, so up to that count the launch takes one warp's
-// time. For fewer rays, each ray is traced by a group of four lanes, one per
+// The rays are few (~0.15% of a sky at 512 steps) and FP64 runs at 1/64 of
+// the FP32 rate: a warp of 32 single-thread FP64 rays needs ~0.17-0.25 s for
+// 512 steps however few of its lanes are busy, so the launch takes about one
+// warp's time. Each ray is therefore traced by a group of four lanes, one per
 // field (B_x, B_y, B_z, phi): every lane interpolates its field, the group
 // exchanges the four results by shuffles, and every lane forms the rest of the
-// right-hand side with the operations of rhs_std<kFP64> in the same order, so
-// the maps are bit-identical to the FP64 trace while a warp issues about a
-// third of the FP64 instructions per step (~3x shorter). Four-lane groups win
-// up to about two warps per sub-partition; both kernels are launched and the
-// one not suited to the list's length returns at once.
+// right-hand side. Short lists run this in FP64 with the operations of
+// rhs_std<kFP64> in the same order (bit-identical maps); long lists run it in
+// double-float arithmetic on the FP32 pipes (srt_dd.cuh; trajectory ~1e-14
+// from the FP64 one, maps within one float ulp), which is shorter once the
+// warps outnumber the SM sub-partitions.
 constexpr int64_t kRefineMaxBlocks = 152 * 32;
 constexpr int64_t kRefineGroupMaxRays = 2 * 608 * 8;
 
@@ -154,14 +154,14 @@ __device__ __forceinline__ void shfl_tri(Tri<double>& d, const Tri<double>& s, i
 __device__ __forceinline__ void rhs_fp64_group(const double* y, double* dy, const FieldPtrs& F, const Geom& G,
                                                int field, int group, unsigned mask) {
   double n[3], a[3], b[3];
-  rhs_frame(y, n, a, b);
+  rhs_frame<double>(y, n, a, b);
   Tri<double> own;
   {
     const float* src = (field == 3) ? F.phi : ((field == 0) ? F.b[0] : ((field == 1) ? F.b[1] : F.b[2]));
     const double ox = (field == 0) ? 0.5 : 0.0, oy = (field == 1) ? 0.5 : 0.0, oz = (field == 2) ? 0.5 : 0.0;
     interp_std<double, float>(src, G, y[0] - ox, y[1] - oy, y[2] - oz, own);
   }
-  BSums<double> B;
+  BSums<double, double> B;
   B.clear();
   Tri<double> r;
 #pragma unroll
@@ -170,7 +170,7 @@ __device__ __forceinline__ void rhs_fp64_group(const double* y, double* dy, cons
     B.add(c, r, n, a, b);
   }
   shfl_tri(r, own, group + 3, mask);
-  rhs_finish<double>(y, n, a, b, B, r, dy);
+  rhs_finish<double, double>(y, n, a, b, B, r, dy);
 }
 
 // step_std<kFP64> on rhs_fp64_group.
@@ -188,13 +188,69 @@ __device__ __forceinline__ void step_fp64_group(const FieldPtrs& F, const Geom& 
   for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) / 6.0;
 }
 
-template <int LANES>
-__global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A) {
+// rhs_dd with the four interpolations spread over a lane group, as
+// rhs_fp64_group does for FP64.
+__device__ __forceinline__ void shfl_tri_dd(Tri<dd>& d, const Tri<dd>& s, int src, unsigned mask) {
+  d.v = dd(__shfl_sync(mask, s.v.hi, src), __shfl_sync(mask, s.v.lo, src));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) d.g[i] = dd(__shfl_sync(mask, s.g[i].hi, src), __shfl_sync(mask, s.g[i].lo, src));
+#pragma unroll
+  for (int i = 0; i < 6; ++i) d.h[i] = dd(__shfl_sync(mask, s.h[i].hi, src), __shfl_sync(mask, s.h[i].lo, src));
+}
+
+__device__ __forceinline__ void rhs_dd_group(const dd* y, dd* dy, const FieldPtrs& F, const Geom& G, int field,
+                                             int group, unsigned mask) {
+  dd n[3], a[3], b[3];
+  rhs_frame<dd>(y, n, a, b);
+  Tri<dd> own;
+  {
+    const float* src = (field == 3) ? F.phi : ((field == 0) ? F.b[0] : ((field == 1) ? F.b[1] : F.b[2]));
+    const dd half(0.5f);
+    interp_dd(src, G, field == 0 ? y[0] - half : y[0], field == 1 ? y[1] - half : y[1],
+              field == 2 ? y[2] - half : y[2], own);
+  }
+  BSums<dd, dd> B;
+  B.clear();
+  Tri<dd> r;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    shfl_tri_dd(r, own, group + c, mask);
+    B.add(c, r, n, a, b);
+  }
+  shfl_tri_dd(r, own, group + 3, mask);
+  rhs_finish<dd, dd>(y, n, a, b, B, r, dy);
+}
+
+__device__ __forceinline__ void step_dd_group(const FieldPtrs& F, const Geom& G, dd* y, int field, int group,
+                                              unsigned mask) {
+  dd acc[19], k[19], ys[19];
+#pragma unroll 1
+  for (int st = 0; st < 4; ++st) {
+    const float c = (st == 3) ? 1.f : 0.5f;
+    for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
+    rhs_dd_group(ys, k, F, G, field, group, mask);
+    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
+  }
+  const dd sixth = dd(1.0 / 6.0);
+  for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
+}
+
+// Which re-trace a list gets: up to dd_min rays the bit-exact FP64 four-lane
+// groups (one warp per sub-partition at most: latency-bound, and FP64 is
+// then the shorter), longer lists double-float four-lane groups (~1.4x
+// shorter than FP64 one-lane warps at ~19k rays, maps within one float ulp of
+// the FP64 ones). The environment variable SRT_REFINE_DD_MIN overrides dd_min
+// (tests use it to reach the double-float path on small skies).
+// MODE 4: FP64, four lanes per ray (lists up to SRT_REFINE_DD_MIN rays);
+// MODE 1: double-float, one lane per ray (longer lists).
+template <int MODE>
+__global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t dd_min) {
+  constexpr int LANES = 4;
   constexpr int kRays = 32 / LANES;  // rays per warp
   const int lane = threadIdx.x;
   const unsigned long long count = *A.refine_count;
   const int64_t n = min((int64_t)count, A.pix_count);
-  if ((LANES == 4) != (n <= kRefineGroupMaxRays)) return;
+  if ((MODE == 4) != (n <= dd_min)) return;
 #pragma unroll 1
   for (int64_t k0 = (int64_t)blockIdx.x * kRays; k0 < n; k0 += (int64_t)gridDim.x * kRays) {
     const int64_t k = k0 + lane / LANES;
@@ -202,21 +258,26 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A) {
     const int64_t o = A.refine_list[k];  // output slot
     const int64_t ring = A.nested ? hp_nest2ring(A.nside, A.pix_begin + o) : A.pix_begin + o;
     const RayDir d = ray_dir_pix(A.nside, ring);
-    double y[19];
-    init_std(d, A.G, y);
-    if (LANES == 4) {
+    float out[6];
+    if (MODE == 4) {
+      double y[19];
+      init_std(d, A.G, y);
       // live groups are a prefix of the warp: their lanes form the shuffle mask
       const int64_t live = min((int64_t)kRays, n - k0);
       const unsigned mask = (live >= kRays) ? 0xffffffffu : ((1u << (4 * live)) - 1u);
 #pragma unroll 1
       for (int step = 0; step < A.n_steps; ++step) step_fp64_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
+      extract_std(d, A.G, y, out);
     } else {
+      dd y[19];
+      init_dd(d, A.G, y);
+      const int64_t live = min((int64_t)kRays, n - k0);
+      const unsigned mask = (live >= kRays) ? 0xffffffffu : ((1u << (4 * live)) - 1u);
 #pragma unroll 1
-      for (int step = 0; step < A.n_steps; ++step) step_std<kFP64>(A.F, A.G, y, nullptr);
+      for (int step = 0; step < A.n_steps; ++step) step_dd_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
+      extract_dd(d, A.G, y, out);
     }
     if (lane % LANES == 0) {
-      float out[6];
-      extract_std(d, A.G, y, out);
 #pragma unroll
       for (int m = 0; m < 6; ++m) A.maps[m][o] = out[m];
     }
@@ -224,11 +285,12 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A) {
 }
 
 cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels) {
-  const int64_t b1 = std::min((a.pix_count + 31) / 32, kRefineMaxBlocks);
-  const int64_t b4 = std::min((std::min(a.pix_count, kRefineGroupMaxRays) + 7) / 8, kRefineMaxBlocks);
-  if (b1 < 1) return cudaSuccess;
-  refine_kernel<4><<<(unsigned)b4, 32, 0, s>>>(a);
-  refine_kernel<1><<<(unsigned)b1, 32, 0, s>>>(a);
+  int64_t dd_min = kRefineGroupMaxRays;
+  if (const char* e = getenv("SRT_REFINE_DD_MIN")) dd_min = strtoll(e, nullptr, 10);
+  const int64_t blocks = std::min((a.pix_count + 7) / 8, kRefineMaxBlocks);
+  if (blocks < 1) return cudaSuccess;
+  refine_kernel<4><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min);
+  refine_kernel<1><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min);
   if (kernels) *kernels += 2;
   return cudaGetLastError();
 }

@@ -40,6 +40,7 @@
 #include <math.h>
 #include <cuda_fp16.h>
 #include "srt_healpix.cuh"
+#include "srt_dd.cuh"
 
 namespace srt {
 
@@ -296,11 +297,17 @@ SRT_HD void interp_std(const TapT* f, const Geom& G, double x, double y, double 
 
 // --------------------------------------------- right-hand side, FP64 / REF16
 
+// Square root of the state type R (double, or the double-float dd).
+SRT_HD double sqrt_r(double x) { return sqrt(x); }
+SRT_HD dd sqrt_r(const dd& x) { return dd_sqrt(x); }
+
 // Unit vectors n, e1, e2 of the full state y (snapshot-raytracer.cu:338-349).
-SRT_HD void rhs_frame(const double* y, double* n, double* a, double* b) {
-  const double rn = sqrt(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
-  const double ra = sqrt(y[6] * y[6] + y[7] * y[7] + y[8] * y[8]);
-  const double rb = sqrt(y[9] * y[9] + y[10] * y[10] + y[11] * y[11]);
+// R: the state's real type (double; dd in the re-trace of flagged rays).
+template <typename R>
+SRT_HD void rhs_frame(const R* y, R* n, R* a, R* b) {
+  const R rn = sqrt_r(y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+  const R ra = sqrt_r(y[6] * y[6] + y[7] * y[7] + y[8] * y[8]);
+  const R rb = sqrt_r(y[9] * y[9] + y[10] * y[10] + y[11] * y[11]);
   for (int i = 0; i < 3; ++i) {
     n[i] = y[3 + i] / rn;
     a[i] = y[6 + i] / ra;
@@ -312,7 +319,7 @@ SRT_HD void rhs_frame(const double* y, double* n, double* a, double* b) {
 // n.grad B, the e.n.grad B scalars, the tidal matrix and n . Laplacian B.
 // The e_i.grad B vectors the reference also forms there are never used and
 // are not computed.
-template <typename IT>
+template <typename IT, typename R = double>
 struct BSums {
   IT val[3], ngB[3], e1ngB, e2ngB, nlap;
   IT T[6];  // xx, xy, xz, yy, yz, zz
@@ -322,24 +329,24 @@ struct BSums {
     for (int i = 0; i < 6; ++i) T[i] = 0;
   }
   // Adds component c's value, gradient and Hessian r.
-  SRT_HD void add(int c, const Tri<IT>& r, const double* n, const double* a, const double* b) {
+  SRT_HD void add(int c, const Tri<IT>& r, const R* n, const R* a, const R* b) {
     val[c] = r.v;
     for (int i = 0; i < 3; ++i) ngB[i] = (IT)(ngB[i] + r.g[i] * n[c]);
-    const double gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
-    const double ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
-    const double gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
+    const R gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
+    const R ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
+    const R gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
     e1ngB = (IT)(e1ngB + 0.5 * a[c] * gn + 0.5 * n[c] * ga);
     e2ngB = (IT)(e2ngB + 0.5 * b[c] * gn + 0.5 * n[c] * gb);
     // H n for this component's Hessian (rows of the symmetric matrix)
-    const double Hn0 = r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2];
-    const double Hn1 = r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2];
-    const double Hn2 = r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2];
-    const double Hn[3] = {Hn0, Hn1, Hn2};
+    const R Hn0 = r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2];
+    const R Hn1 = r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2];
+    const R Hn2 = r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2];
+    const R Hn[3] = {Hn0, Hn1, Hn2};
     // T_ij += n_c H_ij - 1/2 (delta_ci (H n)_j + delta_cj (H n)_i)
     const int kIdx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     for (int i = 0; i < 3; ++i)
       for (int j = i; j < 3; ++j) {
-        double d = r.h[kIdx[i][j]] * n[c];
+        R d = r.h[kIdx[i][j]] * n[c];
         if (i == c) d -= 0.5 * Hn[j];
         if (j == c) d -= 0.5 * Hn[i];
         T[kIdx[i][j]] = (IT)(T[kIdx[i][j]] + d);
@@ -350,47 +357,47 @@ struct BSums {
 
 // The right-hand side from the frame, the B sums and phi's interpolation p
 // (snapshot-raytracer.cu:462-509).
-template <typename IT>
-SRT_HD void rhs_finish(const double* y, const double* n, const double* a, const double* b, const BSums<IT>& B,
-                       const Tri<IT>& p, double* dy) {
-  const double dA = y[12], dAp = y[13], s1 = y[14], s2 = y[15], el1 = y[16], el2 = y[17];
-  const double phi1 = 1.0 + 2.0 * p.v;
+template <typename IT, typename R = double>
+SRT_HD void rhs_finish(const R* y, const R* n, const R* a, const R* b, const BSums<IT, R>& B, const Tri<IT>& p,
+                       R* dy) {
+  const R dA = y[12], dAp = y[13], s1 = y[14], s2 = y[15], el1 = y[16], el2 = y[17];
+  const R phi1 = 1.0 + 2.0 * p.v;
   for (int i = 0; i < 3; ++i) dy[i] = -n[i] * phi1 - B.val[i];
   // -P_perp v with P_perp = n n^T - I  ->  v - n (n.v)
-  const double v0 = 2.0 * p.g[0] + B.ngB[0], v1 = 2.0 * p.g[1] + B.ngB[1], v2 = 2.0 * p.g[2] + B.ngB[2];
-  const double nv = n[0] * v0 + n[1] * v1 + n[2] * v2;
+  const R v0 = 2.0 * p.g[0] + B.ngB[0], v1 = 2.0 * p.g[1] + B.ngB[1], v2 = 2.0 * p.g[2] + B.ngB[2];
+  const R nv = n[0] * v0 + n[1] * v1 + n[2] * v2;
   dy[3] = v0 - n[0] * nv;
   dy[4] = v1 - n[1] * nv;
   dy[5] = v2 - n[2] * nv;
-  const double ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
-  const double bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
+  const R ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
+  const R bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
   for (int i = 0; i < 3; ++i) {
     dy[6 + i] = -2.0 * n[i] * ag - n[i] * B.e1ngB;
     dy[9 + i] = -2.0 * n[i] * bg - n[i] * B.e2ngB;
   }
-  const double L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
+  const R L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
                    0.25 * (n[0] * B.ngB[0] + n[1] * B.ngB[1] + n[2] * B.ngB[2]);
   // P_perp : H = n^T H n - tr H
-  const double nHn = n[0] * n[0] * p.h[0] + n[1] * n[1] * p.h[3] + n[2] * n[2] * p.h[5] +
+  const R nHn = n[0] * n[0] * p.h[0] + n[1] * n[1] * p.h[3] + n[2] * n[2] * p.h[5] +
                      2.0 * (n[0] * n[1] * p.h[1] + n[0] * n[2] * p.h[2] + n[1] * n[2] * p.h[4]);
-  const double PH = nHn - (p.h[0] + p.h[3] + p.h[5]);
+  const R PH = nHn - (p.h[0] + p.h[3] + p.h[5]);
   dy[12] = -dAp;
   dy[13] = -4.0 * dAp * L - PH * dA + 0.5 * B.nlap * dA;
   // effective tidal matrix H + T/2 projected on the shear basis
   IT He[6];
   for (int i = 0; i < 6; ++i) He[i] = (IT)(p.h[i] + 0.5 * B.T[i]);
-  const double S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
+  const R S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
                     (a[2] * a[2] - b[2] * b[2]) * He[5] +
                     2.0 * ((a[0] * a[1] - b[0] * b[1]) * He[1] + (a[0] * a[2] - b[0] * b[2]) * He[2] +
                            (a[1] * a[2] - b[1] * b[2]) * He[4]);
-  const double S2 = 2.0 * (a[0] * b[0] * He[0] + a[1] * b[1] * He[3] + a[2] * b[2] * He[5]) +
+  const R S2 = 2.0 * (a[0] * b[0] * He[0] + a[1] * b[1] * He[3] + a[2] * b[2] * He[5]) +
                     2.0 * ((a[0] * b[1] + a[1] * b[0]) * He[1] + (a[0] * b[2] + a[2] * b[0]) * He[2] +
                            (a[1] * b[2] + a[2] * b[1]) * He[4]);
   dy[14] = 4.0 * s1 * L + S1 * dA * dA;
   dy[15] = 4.0 * s2 * L + S2 * dA * dA;
   if (dA > 0.5) {
-    const double dA2 = dA * dA;
-    const double q = sqrt(4.0 + el1 * el1 + el2 * el2);
+    const R dA2 = dA * dA;
+    const R q = sqrt_r(4.0 + el1 * el1 + el2 * el2);
     dy[13] += (s1 * s1 + s2 * s2) / (dA2 * dA);
     dy[16] = -2.0 * s1 * q / dA2;
     dy[17] = -2.0 * s2 * q / dA2;
@@ -513,6 +520,137 @@ SRT_HD void trace_ray_std(const FieldPtrs& F, const Geom& G, const RayDir& d, in
 #pragma unroll 1
   for (int step = 0; step < n_steps; ++step) step_std<MODE>(F, G, y, nullptr);
   extract_std(d, G, y, out);
+}
+
+// ------------------------------------------- double-float (dd) ray driver
+//
+// The FP64 scheme above in double-float arithmetic (srt_dd.cuh), for the
+// re-trace of the MIXED form's flagged rays: the same state, stages and
+// right-hand side (rhs_frame, BSums, rhs_finish instantiated with dd), the
+// interpolation's dot products accumulated in the compensated form of Ogita,
+// Rump and Oishi ("Accurate sum and dot product", 2005). The trajectory stays
+// ~1e-14 from the FP64 one, far inside the guard's margin.
+
+// Compensated accumulator: s + c, products added with their rounding errors.
+struct DdAcc {
+  float s = 0.f, c = 0.f;
+  SRT_HD void add(const dd& w, float x) {  // += w * x
+    const float p = w.hi * x;
+    const float e = fmaf(w.hi, x, -p);
+    float t, q;
+    dd_two_sum(s, p, t, q);
+    s = t;
+    c += fmaf(w.lo, x, e + q);
+  }
+  SRT_HD void add(const dd& w, const dd& x) {  // += w * x
+    const float p = w.hi * x.hi;
+    const float e = fmaf(w.hi, x.hi, -p);
+    float t, q;
+    dd_two_sum(s, p, t, q);
+    s = t;
+    c += fmaf(w.hi, x.lo, fmaf(w.lo, x.hi, e + q));
+  }
+  SRT_HD dd value() const {
+    float h, l;
+    dd_fast_two_sum(s, c, h, l);
+    return dd(h, l);
+  }
+};
+
+// tricubic<dd, float>: the same passes with compensated accumulation.
+SRT_HD void tricubic_dd(const float* __restrict__ f, int64_t base, int64_t px, int64_t pxy, const CRW<dd>& X,
+                        const CRW<dd>& Y, const CRW<dd>& Z, Tri<dd>& r) {
+  DdAcc v, g0, g1, g2, h00, h01, h02, h11, h12, h22;
+#pragma unroll 1
+  for (int c = 0; c < 4; ++c) {
+    DdAcc a, ay, ayy, ax, axy, axx;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const float* row = f + base + c * pxy + b * px;
+      const float p[4] = {ldg(row), ldg(row + 1), ldg(row + 2), ldg(row + 3)};
+      DdAcc rv, rx, rxx;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        rv.add(X.w[i], p[i]);
+        rx.add(X.g[i], p[i]);
+        rxx.add(X.h[i], p[i]);
+      }
+      const dd RV = rv.value(), RX = rx.value(), RXX = rxx.value();
+      a.add(Y.w[b], RV);
+      ay.add(Y.g[b], RV);
+      ayy.add(Y.h[b], RV);
+      ax.add(Y.w[b], RX);
+      axy.add(Y.g[b], RX);
+      axx.add(Y.w[b], RXX);
+    }
+    const dd A = a.value(), AY = ay.value(), AYY = ayy.value(), AX = ax.value(), AXY = axy.value(),
+             AXX = axx.value();
+    v.add(Z.w[c], A);
+    g0.add(Z.w[c], AX);
+    g1.add(Z.w[c], AY);
+    g2.add(Z.g[c], A);
+    h00.add(Z.w[c], AXX);
+    h01.add(Z.w[c], AXY);
+    h02.add(Z.g[c], AX);
+    h11.add(Z.w[c], AYY);
+    h12.add(Z.g[c], AY);
+    h22.add(Z.h[c], A);
+  }
+  r.v = v.value();
+  r.g[0] = g0.value();
+  r.g[1] = g1.value();
+  r.g[2] = g2.value();
+  r.h[0] = h00.value();
+  r.h[1] = h01.value();
+  r.h[2] = h02.value();
+  r.h[3] = h11.value();
+  r.h[4] = h12.value();
+  r.h[5] = h22.value();
+}
+
+// interp_std<double, float> in dd: cell from the dd position, dd offsets.
+SRT_HD void interp_dd(const float* f, const Geom& G, const dd& x, const dd& y, const dd& z, Tri<dd>& r) {
+  const dd fx = dd_floor(x), fy = dd_floor(y), fz = dd_floor(z);
+  const int64_t ix = (int64_t)fx.hi + (int64_t)fx.lo, iy = (int64_t)fy.hi + (int64_t)fy.lo,
+                iz = (int64_t)fz.hi + (int64_t)fz.lo;
+  CRW<dd> X, Y, Z;
+  cr_weights(x - fx, X);
+  cr_weights(y - fy, Y);
+  cr_weights(z - fz, Z);
+  const int64_t base = cell_base(G, wrap64(ix, G.n[0]), wrap64(iy, G.n[1]), wrap64(iz, G.n[2]));
+  tricubic_dd(f, base, G.px, G.pxy, X, Y, Z, r);
+}
+
+// rhs_std<kFP64> in dd.
+SRT_HD void rhs_dd(const dd* y, dd* dy, const FieldPtrs& F, const Geom& G) {
+  dd n[3], a[3], b[3];
+  rhs_frame<dd>(y, n, a, b);
+  BSums<dd, dd> B;
+  B.clear();
+  const dd half(0.5f);
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    Tri<dd> r;
+    interp_dd(F.b[c], G, c == 0 ? y[0] - half : y[0], c == 1 ? y[1] - half : y[1], c == 2 ? y[2] - half : y[2], r);
+    B.add(c, r, n, a, b);
+  }
+  Tri<dd> p;
+  interp_dd(F.phi, G, y[0], y[1], y[2], p);
+  rhs_finish<dd, dd>(y, n, a, b, B, p, dy);
+}
+
+// init_std / extract_std in dd (the step is step_dd_group in srt_kernels.cu).
+SRT_HD void init_dd(const RayDir& d, const Geom& G, dd* y) {
+  double y64[19];
+  init_std(d, G, y64);
+  for (int j = 0; j < 19; ++j) y[j] = dd(y64[j]);
+}
+
+
+SRT_HD void extract_dd(const RayDir& d, const Geom& G, const dd* y, float out[6]) {
+  double y64[19];
+  for (int j = 0; j < 19; ++j) y64[j] = (double)y[j];
+  extract_std(d, G, y64, out);
 }
 
 // -------------------------------------------------------------- MIXED mode

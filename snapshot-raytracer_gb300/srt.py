@@ -72,6 +72,11 @@ def lib():
                                            ctypes.POINTER(Stats)]),
             "srt_vjp": (ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, ctypes.c_int, _FP6, _P, _P, ctypes.c_int,
                                        ctypes.c_uint, _P, ctypes.POINTER(Stats)]),
+            "srt_forward_tape": (ctypes.c_int, [_P, _I64, _I64, _I64, ctypes.c_int, ctypes.c_int, _FP6, ctypes.c_uint,
+                                                _P, ctypes.POINTER(Stats), ctypes.POINTER(_P)]),
+            "srt_vjp_tape": (ctypes.c_int, [_P, _FP6, _P, _P, ctypes.c_uint, _P, ctypes.POINTER(Stats)]),
+            "srt_tape_bytes": (_I64, [_P]),
+            "srt_tape_destroy": (ctypes.c_int, [_P]),
             "srt_probe_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
             "srt_pix2ang_ring": (ctypes.c_int, [_I64, _I64, ctypes.POINTER(ctypes.c_double),
                                                 ctypes.POINTER(ctypes.c_double)]),
@@ -229,30 +234,95 @@ class Fields:
         npix = 12 * nside * nside
         if pix_count is None:
             pix_count = npix - pix_begin
-        wrt = tuple(wrt)
-        if not wrt or any(w not in ("phi", "b") for w in wrt):
-            raise ValueError("wrt must name 'phi' and/or 'b', got %r" % (wrt,))
-        n0, n1, n2 = self.n
-        if "phi" not in wrt:
-            dphi = None
-        elif dphi is None:
-            dphi = np.zeros((n2, n1, n0), np.float32)
-        if "b" not in wrt:
-            db_xyz = None
-        elif db_xyz is None:
-            db_xyz = np.zeros((n2, n1, n0, 3), np.float32)
-        pw, wdev = _ptr(weights, False)
-        pg, gdev = _ptr(dphi, False) if dphi is not None else (None, wdev)
-        pb, bdev = _ptr(db_xyz, False) if db_xyz is not None else (None, wdev)
-        if not (wdev == gdev == bdev):
-            raise ValueError("weights and gradients must all be host or all be device buffers")
-        rows = _FP6(*[pw + m * pix_count * 4 for m in range(6)])
-        flags = (SRT_OUTPUT_DEVICE if wdev else 0) | (SRT_ACCUMULATE if accumulate else 0) | \
-            (SRT_DETERMINISTIC if deterministic else 0)
+        dphi, db_xyz, rows, pg, pb, flags = _grad_args(self.n, weights, pix_count, dphi, db_xyz, wrt, accumulate,
+                                                       deterministic)
         st = Stats()
         _check(lib().srt_vjp(self._h, nside, pix_begin, pix_count, n_steps, PRECISION[precision], rows, pg, pb,
                              ckpt_every, flags, _stream_ptr(stream), ctypes.byref(st)))
         return dphi, db_xyz, st
+
+    def forward_tape(self, nside, n_steps, pix_begin=0, pix_count=None, ckpt_every=0, out=None, stream=None):
+        """The MIXED forward keeping its checkpoints (srt_forward_tape): the
+        maps of forward() and a Tape whose vjp() needs no forward pass of its
+        own. Returns (maps, Tape, Stats)."""
+        npix = 12 * nside * nside
+        if pix_count is None:
+            pix_count = npix - pix_begin
+        if out is None:
+            out = np.zeros((6, max(pix_count, 0)), np.float32)
+        p, dev = _ptr(out, False)
+        if tuple(out.shape) != (6, pix_count):
+            raise ValueError("out must have shape (6, %d)" % pix_count)
+        rows = _FP6(*[p + m * pix_count * 4 for m in range(6)])
+        st = Stats()
+        h = _P()
+        _check(lib().srt_forward_tape(self._h, nside, pix_begin, pix_count, n_steps, ckpt_every, rows,
+                                      SRT_OUTPUT_DEVICE if dev else 0, _stream_ptr(stream), ctypes.byref(st),
+                                      ctypes.byref(h)))
+        return out, Tape(self, h, pix_count), st
+
+
+def _grad_args(n, weights, pix_count, dphi, db_xyz, wrt, accumulate, deterministic):
+    """Gradient buffers, weight rows, pointers and flags of a vjp call."""
+    wrt = tuple(wrt)
+    if not wrt or any(w not in ("phi", "b") for w in wrt):
+        raise ValueError("wrt must name 'phi' and/or 'b', got %r" % (wrt,))
+    n0, n1, n2 = n
+    if "phi" not in wrt:
+        dphi = None
+    elif dphi is None:
+        dphi = np.zeros((n2, n1, n0), np.float32)
+    if "b" not in wrt:
+        db_xyz = None
+    elif db_xyz is None:
+        db_xyz = np.zeros((n2, n1, n0, 3), np.float32)
+    pw, wdev = _ptr(weights, False)
+    pg, gdev = _ptr(dphi, False) if dphi is not None else (None, wdev)
+    pb, bdev = _ptr(db_xyz, False) if db_xyz is not None else (None, wdev)
+    if not (wdev == gdev == bdev):
+        raise ValueError("weights and gradients must all be host or all be device buffers")
+    rows = _FP6(*[pw + m * pix_count * 4 for m in range(6)])
+    flags = (SRT_OUTPUT_DEVICE if wdev else 0) | (SRT_ACCUMULATE if accumulate else 0) | \
+        (SRT_DETERMINISTIC if deterministic else 0)
+    return dphi, db_xyz, rows, pg, pb, flags
+
+
+class Tape:
+    """Checkpoints of a Fields.forward_tape() call (srt_tape); vjp() sweeps
+    them back. Keeps its Fields alive."""
+
+    def __init__(self, fields, h, pix_count):
+        self.fields, self._h, self.pix_count = fields, h, pix_count
+
+    @property
+    def nbytes(self):
+        return lib().srt_tape_bytes(self._h)
+
+    def vjp(self, weights, dphi=None, db_xyz=None, accumulate=False, deterministic=False, stream=None,
+            wrt=("phi", "b")):
+        """srt_vjp_tape: as Fields.vjp with the tape's arguments (MIXED)."""
+        dphi, db_xyz, rows, pg, pb, flags = _grad_args(self.fields.n, weights, self.pix_count, dphi, db_xyz, wrt,
+                                                       accumulate, deterministic)
+        st = Stats()
+        _check(lib().srt_vjp_tape(self._h, rows, pg, pb, flags, _stream_ptr(stream), ctypes.byref(st)))
+        return dphi, db_xyz, st
+
+    def close(self):
+        if self._h:
+            lib().srt_tape_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def trace(phi, b_xyz, nside, n_steps, batch=None, precision="mixed"):

@@ -25,7 +25,7 @@ def test_exports_every_declared_symbol(srt):
 
 
 def test_abi_version(srt):
-    assert srt.lib().srt_abi_version() == 2
+    assert srt.lib().srt_abi_version() == 3
 
 
 def test_forward_rejects_bad_arguments(srt):

@@ -218,3 +218,23 @@ def test_nested_range_matches_ring(srt, precision):
             assert np.array_equal(got.view(np.uint32), full[:, ring].view(np.uint32))
         with pytest.raises(srt.SrtError):
             f.forward(6, steps, 0, 36, precision=precision, nested=True)
+
+
+def test_mixed_refine_double_float_path(srt, monkeypatch):
+    """Long re-trace lists run in double-float arithmetic (forced here with
+    SRT_REFINE_DD_MIN=0 on a small sky): the re-traced rays agree with the
+    FP64 form to a float ulp or two, everything else is untouched."""
+    phi, b = srt_fields.gaussian_fields_np(128, seed=13)
+    nside, steps = 32, 128
+    with srt.Fields(phi, b) as f:
+        m64, _ = f.forward(nside, steps, precision="fp64")
+        mn, _ = f.forward(nside, steps, precision="mixed", refine=False)
+        monkeypatch.setenv("SRT_REFINE_DD_MIN", "0")
+        mr, st = f.forward(nside, steps, precision="mixed")
+        monkeypatch.delenv("SRT_REFINE_DD_MIN")
+    assert st.refined_rays > 0
+    changed = np.any(mr.view(np.uint32) != mn.view(np.uint32), axis=0)
+    assert changed.sum() <= st.refined_rays
+    # float ulps between the re-traced maps and the FP64 ones
+    ulps = np.abs(mr[:, changed].view(np.int32).astype(np.int64) - m64[:, changed].view(np.int32).astype(np.int64))
+    assert ulps.max() <= 4, ulps.max()

@@ -144,3 +144,27 @@ def test_vjp_accumulate_phi_only_and_ranges(srt):
         assert not np.any(gz) and not np.any(bz)
         with pytest.raises(srt.SrtError):
             f.vjp(nside, steps, w, precision="ref16")
+
+
+def test_forward_tape_vjp_pair(srt):
+    """srt_forward_tape gives srt_forward's maps and keeps the checkpoints;
+    srt_vjp_tape then gives srt_vjp's gradient (bit for bit in the
+    deterministic mode) without a forward pass, as often as wanted."""
+    phi, b, nside, steps, w = _case(n=24, nside=4, steps=14, seed=2)
+    lo, cnt = 37, 120
+    wpart = np.ascontiguousarray(w[:, lo:lo + cnt])
+    with srt.Fields(phi, b) as f:
+        m, _ = f.forward(nside, steps, lo, cnt, precision="mixed")
+        mt, tape, st = f.forward_tape(nside, steps, lo, cnt, ckpt_every=5)
+        assert np.array_equal(mt.view(np.uint32), m.view(np.uint32))
+        assert tape.nbytes >= (14 // 5 + 2) * 38 * 4 * cnt
+        g1, b1, _ = f.vjp(nside, steps, wpart, lo, cnt, precision="mixed", deterministic=True, ckpt_every=5)
+        g2, b2, s2 = tape.vjp(wpart, deterministic=True)
+        assert np.array_equal(g2.view(np.uint32), g1.view(np.uint32))
+        assert np.array_equal(b2.view(np.uint32), b1.view(np.uint32))
+        assert s2.kernels < 2 * (14 // 5 + 1) + 8
+        g3, _, _ = tape.vjp(2 * wpart, deterministic=True, wrt=("phi",))
+        assert np.allclose(g3, 2 * g1, rtol=1e-6, atol=1e-6 * np.abs(g1).max())
+        ga, ba, _ = tape.vjp(wpart)  # FP32 atomics
+        assert np.abs(ga - g1).max() <= 1e-4 * np.abs(g1).max()
+        tape.close()
