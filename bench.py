@@ -408,7 +408,8 @@ def run_ours(args):
         del phi_d, b_d
         torch.cuda.empty_cache()
         phi_np, b_np = phi_h.numpy(), b_h.numpy()
-        maps_h = np.zeros((6, npix), np.float32)
+        # the maps land in pinned host memory, as the inputs come from it
+        maps_h = torch.zeros((6, npix), dtype=torch.float32, pin_memory=True).numpy()
         times = []
         for i in range(args.e2e_steps + 1):
             barrier(world)

@@ -142,9 +142,9 @@ int64_t srt_fields_bytes(const srt_fields* fields);
  * Rays are set up from the pixel centres and the observer at the box centre on
  * the device and launched in NESTED order for locality; results are stored at
  * their RING index. MIXED traces in FP32 and re-traces in FP64 the few rays
- * (~0.15% at 512 steps) whose stage positions pass a cell face closer than
- * the FP32 trajectory's error bound, 4e-7 (max|dx| + s max|dn|) + 1e-10 grid
- * units, where the FP32 and FP64 trajectories could pick different cells (the
+ * (~0.1% at 512 steps) whose stage positions pass a cell face closer than
+ * the FP32 trajectory's error bound, 4e-7 (s max|dn| + 1e-3) grid units at
+ * affine distance s, where the FP32 and FP64 trajectories could pick different cells (the
  * Catmull-Rom Hessian jumps across faces); those rays then equal the FP64
  * result bit for bit (SRT_MIXED_NO_REFINE skips this). The CLI's batch b is
  * pix_begin = b*nside^2, pix_count = nside^2 (snapshot-raytracer.cu:708-717);

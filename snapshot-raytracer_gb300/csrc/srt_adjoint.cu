@@ -120,11 +120,11 @@ __global__ void __launch_bounds__(128, MAPS ? 2 : 1) ckpt_kernel_mixed(const Adj
   store_vec(ck, A.count, slot, y, kMixedState);
   // MAPS: the guard of the trace kernel; else disabled (cell-face proximity
   // matters for the maps, not for the gradient)
-  __shared__ float guard_m[MAPS ? 128 : 1][3];
+  __shared__ float guard_m[MAPS ? 128 : 1][2];
   Guard gd;
   if (MAPS) {
     gd.m = guard_m[threadIdx.x];
-    gd.m[0] = gd.m[1] = 0.f;
+    gd.m[0] = 0.f;
   }
 #pragma unroll 1
   for (int st = 0; st < A.n_steps; ++st) {

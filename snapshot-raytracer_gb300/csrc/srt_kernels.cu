@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ?
   const RayDir d = ray_dir_pix(A.nside, ring);
   float out[6];
   if (MODE == kMIXED_PAIR || MODE == kMIXED) {
-    __shared__ float guard_m[128][3];  // the ray's guard state, out of the register budget
+    __shared__ float guard_m[128][2];  // the ray's guard state, out of the register budget
     const bool near = trace_ray_mixed<MODE == kMIXED_PAIR>(A.F, A.G, d, A.n_steps, out, guard_m[threadIdx.x]);
     if (near && A.refine_list) {
       const unsigned long long k = atomicAdd(A.refine_count, 1ull);

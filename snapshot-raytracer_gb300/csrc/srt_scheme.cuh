@@ -745,15 +745,19 @@ SRT_HD void add_b_component(const FieldPtrs& F, const Geom& G, const int* cc, co
 // Cell-face guard. Catmull-Rom's Hessian jumps across cell faces, so where
 // the FP32 and FP64 trajectories pass a face on different sides the maps of
 // that ray differ by up to ~1% of their rms. The FP32 trajectory's distance
-// from the FP64 one was measured on the GPU, stage by stage (256^3 and 512^3
-// Gaussian fields, 256 steps, 295k rays), against the running maxima of the
-// perturbation, Mx = max |dx| and Mn = max |dn| over the path so far:
-// |x32 - x64| <= k (Mx + s Mn) with k below 8e-8 for half the rays, below
-// 2e-7 for 99% and below 3.7e-7 for all. A stage whose position lies within
-// g = kFaceGuardRel (Mx + s Mn) + kFaceGuardAbs of a cell face (either face,
-// centred or staggered grid) marks the ray for an FP64 re-trace.
+// from the FP64 one was measured on the GPU, stage by stage (a lockstep
+// FP64 / MIXED kernel: 256^3 / 256 steps / 49k rays, 512^3 / 512 steps / 49k
+// rays, 1024^3 / 1024 steps / 12k rays) against candidate bounds; the one that
+// holds with the smallest margin is s Mn, the affine distance times the
+// running maximum Mn = max |dn| of the direction perturbation:
+// |x32 - x64| <= k (s Mn + 1e-3) with k below 1.6e-7 for 99% of the rays and
+// below 3.3e-7 for all, at every length (a bound that also carries
+// Mx = max |dx| needed k up to 5.5e-7 at 1024 steps and flags 2-3x more rays).
+// A stage whose position lies within g = kFaceGuardRel (s Mn + kFaceGuardFloor)
+// of a cell face (either face, centred or staggered grid) marks the ray for
+// an FP64 re-trace.
 constexpr float kFaceGuardRel = 4e-7f;
-constexpr float kFaceGuardAbs = 1e-10f;
+constexpr float kFaceGuardFloor = 1e-3f;
 // No guard is needed for the dA > 1/2 switch (snapshot-raytracer.cu:497): dA
 // passes 1/2 inside the first step, where dA - 1/2 at the midpoint stages is
 // either exactly 0 in both precisions (the switch is off in both) or ~k2/2 ~
@@ -761,28 +765,24 @@ constexpr float kFaceGuardAbs = 1e-10f;
 // sign; and were they to differ, the switched terms are proportional to the
 // shear, which is 0 at the start of the ray.
 
-// Per-ray guard state: the flag, and (through m, three floats the caller
+// Per-ray guard state: the flag, and (through m, two floats the caller
 // provides; the trace kernel keeps them in shared memory, out of the register
-// budget) the running maxima Mx = max |dx| and Mn = max |dn| taken at the
-// start of each step and the smallest distance dmin of the step's stage
-// positions from a cell face. A step is flagged when
-// dmin < kFaceGuardRel (Mx + s_end Mn) + kFaceGuardAbs, s_end the step's end.
-// Guard{} (m null) is disabled.
+// budget) the running maximum Mn = max |dn| taken at the start of each step
+// and the smallest distance dmin of the step's stage positions from a cell
+// face. A step is flagged when dmin < kFaceGuardRel (s_end Mn +
+// kFaceGuardFloor), s_end the step's end. Guard{} (m null) is disabled.
 struct Guard {
   bool near = false;
   float* m = nullptr;
   SRT_HD void begin_step(const float* y) {
-    m[0] = fmaxf(m[0], fmaxf(fabsf(y[0]), fmaxf(fabsf(y[1]), fabsf(y[2]))));
-    m[1] = fmaxf(m[1], fmaxf(fabsf(y[3]), fmaxf(fabsf(y[4]), fabsf(y[5]))));
-    m[2] = 1.f;
+    m[0] = fmaxf(m[0], fmaxf(fabsf(y[3]), fmaxf(fabsf(y[4]), fabsf(y[5]))));
+    m[1] = 1.f;
   }
   // a stage's smallest distance from a face
   SRT_HD void face(float d) {
-    if (m) m[2] = fminf(m[2], d);
+    if (m) m[1] = fminf(m[1], d);
   }
-  SRT_HD void end_step(int step) {
-    near |= m[2] < kFaceGuardRel * (m[0] + (float)(step + 1) * m[1]) + kFaceGuardAbs;
-  }
+  SRT_HD void end_step(int step) { near |= m[1] < kFaceGuardRel * ((float)(step + 1) * m[0] + kFaceGuardFloor); }
 };
 
 // Distance of offset t from the nearer face; 1 - t is 0 where t rounded to 1
@@ -949,7 +949,7 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
     rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k, gd);
     // at s = 0 the ray sits exactly on the observer (a grid node, offsets
     // exactly 0) in both precisions, so no cell choice can differ there
-    if (step == 0 && st == 0 && gd.m) gd.m[2] = 1.f;
+    if (step == 0 && st == 0 && gd.m) gd.m[1] = 1.f;
     for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
   }
   for (int j = 0; j < kCompensated; ++j) {
@@ -994,7 +994,7 @@ SRT_HD bool trace_ray_mixed(const FieldPtrs& F, const Geom& G, const RayDir& d, 
   init_mixed(d, R, y);
   Guard gd;
   gd.m = guard_m;
-  gd.m[0] = gd.m[1] = 0.f;
+  gd.m[0] = 0.f;
 #pragma unroll 1
   for (int step = 0; step < n_steps; ++step) {
     gd.begin_step(y);
