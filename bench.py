@@ -410,20 +410,28 @@ def run_ours(args):
         phi_np, b_np = phi_h.numpy(), b_h.numpy()
         # the maps land in pinned host memory, as the inputs come from it
         maps_h = torch.zeros((6, npix), dtype=torch.float32, pin_memory=True).numpy()
-        times = []
+        times, split = [], []
         for i in range(args.e2e_steps + 1):
             barrier(world)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            with srt.Fields(phi_np, b_np) as f:
-                f.forward(nside, S, precision=args.precision, out=maps_h)
+            f = srt.Fields(phi_np, b_np)
+            ta = time.perf_counter()
+            f.forward(nside, S, precision=args.precision, out=maps_h)
+            tb = time.perf_counter()
+            f.close()
             t1 = time.perf_counter()
             if i > 0:
                 times.append(t1 - t0)
+                split.append(((ta - t0) * 1e3, (tb - ta) * 1e3, (t1 - tb) * 1e3))
         e2e_s = max_over_ranks(float(np.mean(times)), world)
+        sp = np.mean(np.array(split), axis=0)
         result["e2e"] = {"value": world * ray_steps / e2e_s, "unit": "ray-steps/s",
                          "h2d_bytes_per_step": int(phi_np.nbytes + b_np.nbytes),
-                         "d2h_bytes_per_step": int(maps_h.nbytes), "ms_per_step": e2e_s * 1e3}
+                         "d2h_bytes_per_step": int(maps_h.nbytes), "ms_per_step": e2e_s * 1e3,
+                         "split_ms": {"fields_create_upload": float(sp[0]), "forward_and_maps_back": float(sp[1]),
+                                      "fields_release": float(sp[2])},
+                         "create_ms_each": [round(x[0], 1) for x in split]}
         fields = srt.Fields(phi_np, b_np)
     else:
         phi_np = b_np = None

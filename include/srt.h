@@ -133,6 +133,13 @@ int srt_fields_destroy(srt_fields* fields);
 /* Device bytes held by a fields handle. */
 int64_t srt_fields_bytes(const srt_fields* fields);
 
+/* Field memory comes from a per-device pool that keeps what srt_fields_destroy
+ * hands back, so that the next srt_fields_create of the same size is not slowed
+ * down by the driver mapping tens of GB again. This returns the pool's unused
+ * memory to the device (a failed allocation also does, before retrying). No
+ * counterpart in the reference. */
+int srt_release_cached_memory(void);
+
 /* -------------------------------------------------------------- forward */
 
 /* Trace one ray per HEALPix RING pixel p in [pix_begin, pix_begin+pix_count)

@@ -5,11 +5,83 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include "srt_internal.h"
 
 namespace {
 thread_local std::string g_last_error;
+
+// Device memory of the fields (and of their upload slabs): a stream-ordered
+// pool per device that keeps what is handed back (release threshold:
+// unlimited), so that creating fields of the same size again reuses the
+// mapped memory instead of paying the driver's mapping cost (~0.3 s for the
+// 52 GB of a 1024^3 handle). A failed allocation trims the pool and retries
+// once; srt_release_cached_memory() trims it on request.
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pool[kMaxPoolDevices] = {};
+
+cudaError_t device_pool(int dev, cudaMemPool_t* out) {
+  if (dev < 0 || dev >= kMaxPoolDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return e;
+    }
+    g_pool[dev] = pool;
+  }
+  *out = g_pool[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+namespace srt {
+
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  cudaMemPool_t pool = nullptr;
+  if (e == cudaSuccess) e = device_pool(dev, &pool);
+  if (e != cudaSuccess) return e;
+  e = cudaMallocFromPoolAsync(p, bytes ? bytes : 1, pool, s);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    cudaStreamSynchronize(s);
+    cudaMemPoolTrimTo(pool, 0);
+    e = cudaMallocFromPoolAsync(p, bytes ? bytes : 1, pool, s);
+  }
+  return e;
+}
+
+void pool_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+// Bytes the device's pool holds but does not use (reusable by pool_alloc).
+int64_t pool_reusable_bytes(int dev) {
+  cudaMemPool_t pool = nullptr;
+  if (device_pool(dev, &pool) != cudaSuccess) return 0;
+  uint64_t reserved = 0, used = 0;
+  if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess ||
+      cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess)
+    return 0;
+  return reserved > used ? (int64_t)(reserved - used) : 0;
+}
+
+}  // namespace srt
+
+namespace {
 
 struct HostTimer {
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
@@ -87,8 +159,8 @@ using namespace srt;
 
 namespace {
 // The upload's staging slabs, copy stream and events (each may be null).
-void release_upload(float*& slab, cudaStream_t& cs, cudaEvent_t* copied, cudaEvent_t* padded) {
-  if (slab) cudaFree(slab);
+void release_upload(float*& slab, cudaStream_t& cs, cudaEvent_t* copied, cudaEvent_t* padded, cudaStream_t s) {
+  if (slab) srt::pool_free(slab, s);  // after the last pad kernel on s
   if (cs) cudaStreamDestroy(cs);
   for (int i = 0; i < 2; ++i) {
     if (copied[i]) cudaEventDestroy(copied[i]);
@@ -146,8 +218,8 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
     }
     const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
     const int64_t plane = n0 * n1;
-    SRT_CUDA_TRY(cudaMalloc(&f->phi, pvox * sizeof(float)), "cudaMalloc(phi)");
-    for (int c = 0; c < 3; ++c) SRT_CUDA_TRY(cudaMalloc(&f->b[c], pvox * sizeof(float)), "cudaMalloc(B)");
+    SRT_CUDA_TRY(pool_alloc((void**)&f->phi, pvox * sizeof(float), s), "allocate phi");
+    for (int c = 0; c < 3; ++c) SRT_CUDA_TRY(pool_alloc((void**)&f->b[c], pvox * sizeof(float), s), "allocate B");
     f->bytes = 4 * pvox * (int64_t)sizeof(float);
     if (dev_in) {
       SRT_CUDA_TRY(launch_pad_slab(phi, 1, 0, f->phi, f->n, f->pn, 0, n2, s), "pad phi");
@@ -161,7 +233,7 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
       if (kslab < 1) kslab = 1;
       if (kslab > n2) kslab = n2;
       const int64_t slab_floats = kslab * plane * 3;
-      SRT_CUDA_TRY(cudaMalloc(&slab, 2 * slab_floats * sizeof(float)), "cudaMalloc(slabs)");
+      SRT_CUDA_TRY(pool_alloc((void**)&slab, 2 * slab_floats * sizeof(float), s), "allocate slabs");
       SRT_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
       for (int i = 0; i < 2; ++i) {
         SRT_CUDA_TRY(cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming), "cudaEventCreate");
@@ -193,15 +265,17 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
       }
     }
     if (!(flags & SRT_ASYNC) || slab) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
-    release_upload(slab, cs, copied, padded);
+    release_upload(slab, cs, copied, padded, s);
     if (!(flags & SRT_FIELDS_NO_PAIRS)) {
       // row-pair arrays for the packed MIXED path, when they fit with room to spare
       const int64_t pair_bytes = 4 * f->pn[0] * (f->pn[1] - 1) * f->pn[2] * (int64_t)sizeof(float2);
       size_t free_b = 0, total_b = 0;
-      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && pair_bytes + (int64_t(4) << 30) < (int64_t)free_b) {
+      const bool have = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess;
+      const int64_t avail = (int64_t)free_b + pool_reusable_bytes(f->device);
+      if (have && pair_bytes + (int64_t(4) << 30) < avail) {
         const float* srcs[4] = {f->b[0], f->b[1], f->b[2], f->phi};
         for (int c = 0; c < 4; ++c) {
-          SRT_CUDA_TRY(cudaMalloc(&f->pr[c], pair_bytes / 4), "cudaMalloc(row pairs)");
+          SRT_CUDA_TRY(pool_alloc((void**)&f->pr[c], pair_bytes / 4, s), "allocate row pairs");
           SRT_CUDA_TRY(launch_pair_build(srcs[c], f->pr[c], f->pn, s), "row pairs");
         }
         f->bytes += pair_bytes;
@@ -214,7 +288,7 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
 fail:
   if (cs) cudaStreamSynchronize(cs);
   cudaStreamSynchronize(s);
-  release_upload(slab, cs, copied, padded);
+  release_upload(slab, cs, copied, padded, s);
   srt_fields_destroy(f);
   return rc;
 }
@@ -224,14 +298,37 @@ int srt_fields_destroy(srt_fields* f) {
   int prev = 0;
   cudaGetDevice(&prev);
   if (prev != f->device) cudaSetDevice(f->device);
-  cudaFree(f->phi);
+  // no kernel may still read the fields (cudaFree synchronised the device too)
+  cudaDeviceSynchronize();
+  pool_free(f->phi, 0);
   for (int c = 0; c < 3; ++c) {
-    cudaFree(f->b[c]);
-    cudaFree(f->bh[c]);
+    pool_free(f->b[c], 0);
+    pool_free(f->bh[c], 0);
   }
-  for (int c = 0; c < 4; ++c) cudaFree(f->pr[c]);
+  for (int c = 0; c < 4; ++c) pool_free(f->pr[c], 0);
+  cudaDeviceSynchronize();
   if (prev != f->device) cudaSetDevice(prev);
   delete f;
+  return SRT_OK;
+}
+
+int srt_release_cached_memory(void) {
+  int n = 0;
+  cudaGetDeviceCount(&n);
+  int prev = 0;
+  cudaGetDevice(&prev);
+  for (int d = 0; d < n && d < kMaxPoolDevices; ++d) {
+    cudaMemPool_t pool = nullptr;
+    {
+      std::lock_guard<std::mutex> lock(g_pool_mutex);
+      pool = g_pool[d];
+    }
+    if (!pool) continue;
+    cudaSetDevice(d);
+    cudaDeviceSynchronize();
+    cudaMemPoolTrimTo(pool, 0);
+  }
+  cudaSetDevice(prev);
   return SRT_OK;
 }
 
@@ -280,13 +377,13 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
       const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
       __half* h[3] = {nullptr, nullptr, nullptr};
       cudaError_t e = cudaSuccess;
-      for (int c = 0; c < 3 && e == cudaSuccess; ++c) e = cudaMalloc(&h[c], pvox * sizeof(__half));
+      for (int c = 0; c < 3 && e == cudaSuccess; ++c) e = pool_alloc((void**)&h[c], pvox * sizeof(__half), s);
       for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
         e = launch_quantize_half(f->b[c], h[c], pvox, s);
         ++kernels;
       }
       if (e != cudaSuccess) {
-        for (int c = 0; c < 3; ++c) cudaFree(h[c]);
+        for (int c = 0; c < 3; ++c) pool_free(h[c], s);
         rc = cuda_error(e, "REF16 B planes");
         goto fail;
       }

@@ -21,6 +21,12 @@ struct srt_fields {
 
 namespace srt {
 
+// Device memory of fields: a per-device stream-ordered pool that keeps freed
+// memory for reuse (srt_release_cached_memory trims it).
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
+void pool_free(void* p, cudaStream_t s);
+int64_t pool_reusable_bytes(int dev);
+
 // Error reporting (thread-local last error message).
 int set_error(int code, const char* fmt, ...);
 int cuda_error(cudaError_t e, const char* what);

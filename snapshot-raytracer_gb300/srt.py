@@ -93,6 +93,7 @@ def lib():
             "srt_fits_read_map": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P), ctypes.POINTER(_I64),
                                                  ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_int)]),
             "srt_free": (None, [_P]),
+            "srt_release_cached_memory": (ctypes.c_int, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -100,6 +101,11 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def release_cached_memory():
+    """Return the field memory pool's unused memory to the device."""
+    _check(lib().srt_release_cached_memory())
 
 
 def last_error():

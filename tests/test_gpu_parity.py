@@ -238,3 +238,24 @@ def test_mixed_refine_double_float_path(srt, monkeypatch):
     # float ulps between the re-traced maps and the FP64 ones
     ulps = np.abs(mr[:, changed].view(np.int32).astype(np.int64) - m64[:, changed].view(np.int32).astype(np.int64))
     assert ulps.max() <= 4, ulps.max()
+
+
+def test_fields_memory_pool_reuse_and_release(srt):
+    """Destroyed fields leave their memory in the library's pool, a second
+    handle of the same size reuses it, and srt_release_cached_memory returns it."""
+    torch = pytest.importorskip("torch")
+    phi, b = srt_fields.gaussian_fields_np(64, seed=2)
+    srt.release_cached_memory()  # earlier handles' memory may sit in the pool
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    with srt.Fields(phi, b) as f:
+        nbytes = f.nbytes
+        m1, _ = f.forward(8, 16, precision="mixed")
+    held = free0 - torch.cuda.mem_get_info()[0]
+    assert held >= 0.9 * nbytes  # kept by the pool
+    with srt.Fields(phi, b) as f:
+        m2, _ = f.forward(8, 16, precision="mixed")
+        assert free0 - torch.cuda.mem_get_info()[0] <= held + (64 << 20)  # reused, not allocated again
+    assert np.array_equal(m1.view(np.uint32), m2.view(np.uint32))
+    srt.release_cached_memory()
+    assert free0 - torch.cuda.mem_get_info()[0] <= 0.1 * nbytes + (64 << 20)
