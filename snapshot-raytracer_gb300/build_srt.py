@@ -45,7 +45,11 @@ def _run(cmd, verbose):
 
 def _nvcc_obj(src, verbose):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [NVCC, *GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+    # --use_fast_math (as the reference is built, Makefile:9) touches FP32 only:
+    # approximate division and square root, denormals flushed. The MIXED form's
+    # error-free transformations (two-sum, FMA two-product) are exact either way,
+    # and the FP64 form is unaffected.
+    cmd = [NVCC, *GENCODE, "-lineinfo", "-O3", "--use_fast_math", "-std=c++17", "-Xcompiler", "-fPIC",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

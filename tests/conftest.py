@@ -76,3 +76,39 @@ def has_gpu():
         return srt.device_count() > 0
     except Exception:
         return False
+
+
+def linear_phi_case(n=64, g=(3e-7, -2e-7, 4e-7)):
+    """A potential with constant gradient g around the box centre (B = 0) and
+    the first-order analytic maps of a ray of S steps through it: dn/ds = 2 g_perp
+    gives a deflection D = -S g_perp (defl1 = D.theta_hat, defl2 = D.(sin phi,
+    -cos phi, 0)), dA' = 1 - 4 (n0.g) s gives dA = S - 2 (n0.g) S^2, and the
+    shear and rotation stay 0 (Catmull-Rom reproduces a linear field exactly).
+    Rays of S < n/2 - 3 steps never reach the box faces, where the field jumps."""
+    import numpy as np
+
+    g = np.asarray(g, np.float64)
+    x0 = n / 2
+    i = np.arange(n)
+    phi = (g[0] * (i[None, None, :] - x0) + g[1] * (i[None, :, None] - x0) + g[2] * (i[:, None, None] - x0))
+    b = np.zeros((n, n, n, 3), np.float32)
+
+    def predict(theta, phiang, S):
+        n0 = -np.array([np.sin(theta) * np.cos(phiang), np.sin(theta) * np.sin(phiang), np.cos(theta)])
+        th_hat = np.array([np.cos(theta) * np.cos(phiang), np.cos(theta) * np.sin(phiang), -np.sin(theta)])
+        e2 = np.array([np.sin(phiang), -np.cos(phiang), 0.0])
+        D = -S * (g - n0 * np.dot(n0, g))
+        return S - 2 * np.dot(n0, g) * S * S, np.dot(D, th_hat), np.dot(D, e2)
+
+    return phi.astype(np.float32), b, predict
+
+
+def check_linear_phi_maps(maps, nside, S, predict, pix2ang):
+    import numpy as np
+
+    for p in range(maps.shape[1]):
+        dA, d1, d2 = predict(*pix2ang(nside, p), S)
+        assert abs(maps[0, p] - dA) <= 0.02 * abs(dA - S) + 4e-6, (p, maps[0, p], dA)
+        assert abs(maps[4, p] - d1) <= 2e-3 * abs(d1) + 2e-9, (p, maps[4, p], d1)
+        assert abs(maps[5, p] - d2) <= 2e-3 * abs(d2) + 2e-9, (p, maps[5, p], d2)
+        assert abs(maps[1, p]) < 1e-9 and abs(maps[2, p]) < 1e-9 and abs(maps[3, p]) < 1e-12, p

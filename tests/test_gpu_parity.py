@@ -259,3 +259,16 @@ def test_fields_memory_pool_reuse_and_release(srt):
     assert np.array_equal(m1.view(np.uint32), m2.view(np.uint32))
     srt.release_cached_memory()
     assert free0 - torch.cuda.mem_get_info()[0] <= 0.1 * nbytes + (64 << 20)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "ref16"])
+def test_constant_gradient_potential_analytic(srt, orc, precision):
+    """Every precision against the first-order analytic maps of a
+    constant-gradient potential."""
+    from conftest import check_linear_phi_maps, linear_phi_case
+
+    phi, b, predict = linear_phi_case()
+    nside, S = 4, 24
+    with srt.Fields(phi, b) as f:
+        maps, _ = f.forward(nside, S, precision=precision)
+    check_linear_phi_maps(maps, nside, S, predict, orc.pix2ang_ring)

@@ -107,3 +107,14 @@ def test_ref16_oracle_matches_reference_on_gaussian_fields(orc):
     want = orc.ref_trace(phi, b, 4, 20)
     if X86:
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_constant_gradient_potential_analytic(orc):
+    """FP64 oracle against the first-order analytic deflection and dA of a
+    constant-gradient potential."""
+    from conftest import check_linear_phi_maps, linear_phi_case
+
+    phi, b, predict = linear_phi_case()
+    nside, S = 2, 20
+    maps = orc.trace(phi, b, nside, S, mode="fp64")
+    check_linear_phi_maps(maps, nside, S, predict, orc.pix2ang_ring)
