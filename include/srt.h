@@ -232,7 +232,7 @@ int srt_tape_destroy(srt_tape* tape);
 /* ---------------------------------------------------------- measurement */
 
 /* Measured FMA issue rate of the current GPU (FLOP/s, one FMA = 2 FLOP):
- * kind 0 = FP32, kind 1 = FP64. This is the roofline denominator of the trace
+ * kind 0 = FP32, kind 1 = FP64, kind 2 = packed FP32 pairs (FFMA2). This is the roofline denominator of the trace
  * kernels, which are bound by CUDA-core issue rather than by a tensor core or
  * by HBM. No counterpart in the reference. */
 int srt_probe_peak(int kind, double* flops_per_s);

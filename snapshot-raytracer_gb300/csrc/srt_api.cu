@@ -451,7 +451,7 @@ int64_t srt_ring2nest(int64_t nside, int64_t ipring) {
 }
 
 int srt_probe_peak(int kind, double* flops_per_s) {
-  if (!flops_per_s || (kind != 0 && kind != 1)) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_probe_peak: bad arguments");
+  if (!flops_per_s || kind < 0 || kind > 2) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_probe_peak: bad arguments");
   if (srt_device_count() < 1) return set_error(SRT_ERR_NO_DEVICE, "srt_probe_peak: no CUDA device");
   cudaError_t e = probe_fma(kind, flops_per_s);
   if (e != cudaSuccess) return cuda_error(e, "srt_probe_peak");

@@ -327,6 +327,27 @@ __global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
   if (r == (T)-1.2345) out[0] = r;  // keeps the chains live
 }
 
+// The same with packed pairs: eight independent FFMA2 chains per thread
+// (two FP32 FMAs per instruction, the form the MIXED tricubic uses).
+__global__ void fma2_probe_kernel(float* out, int iters, float a, float b) {
+  const float t = (float)threadIdx.x;
+  float2 x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) x[j] = make_float2(t + j, t - j);
+  const float2 a2 = make_float2(a, a), b2 = make_float2(b, b);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) x[j] = __ffma2_rn(x[j], a2, b2);
+    }
+  }
+  float r = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) r += x[j].x + x[j].y;
+  if (r == -1.2345f) out[0] = r;  // keeps the chains live
+}
+
 cudaError_t probe_fma(int kind, double* flops_per_s) {
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -337,7 +358,7 @@ cudaError_t probe_fma(int kind, double* flops_per_s) {
   e = cudaMalloc(&out, 64);
   if (e != cudaSuccess) return e;
   const int threads = 256, blocks = sms * 8;
-  const int iters = kind == 0 ? 4096 : 64;
+  const int iters = kind == 1 ? 64 : 4096;
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
@@ -346,6 +367,8 @@ cudaError_t probe_fma(int kind, double* flops_per_s) {
     cudaEventRecord(t0);
     if (kind == 0)
       fma_probe_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.999999f, 1e-7f);
+    else if (kind == 2)
+      fma2_probe_kernel<<<blocks, threads>>>((float*)out, iters, 0.999999f, 1e-7f);
     else
       fma_probe_kernel<double><<<blocks, threads>>>((double*)out, iters, 0.999999, 1e-7);
     cudaEventRecord(t1);
@@ -359,7 +382,7 @@ cudaError_t probe_fma(int kind, double* flops_per_s) {
   cudaEventDestroy(t1);
   cudaFree(out);
   if (e != cudaSuccess) return e;
-  const double flops = 2.0 * 8.0 * 16.0 * (double)iters * (double)threads * (double)blocks;
+  const double flops = (kind == 2 ? 2.0 : 1.0) * 2.0 * 8.0 * 16.0 * (double)iters * (double)threads * (double)blocks;
   *flops_per_s = flops / (best * 1e-3);
   return cudaGetLastError();
 }

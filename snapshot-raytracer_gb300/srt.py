@@ -125,9 +125,10 @@ def device_count():
 
 
 def probe_peak(kind):
-    """Measured FMA rate of the current GPU in FLOP/s; kind 'fp32' or 'fp64'."""
+    """Measured FMA rate of the current GPU in FLOP/s; kind 'fp32', 'fp64' or
+    'fp32x2' (packed FFMA2 pairs)."""
     v = ctypes.c_double()
-    _check(lib().srt_probe_peak({"fp32": 0, "fp64": 1}[kind], ctypes.byref(v)))
+    _check(lib().srt_probe_peak({"fp32": 0, "fp64": 1, "fp32x2": 2}[kind], ctypes.byref(v)))
     return v.value
 
 
