@@ -28,10 +28,14 @@ struct CRW4 {  // Catmull-Rom weights for value and d/dt .. d3/dt3
   T w[4], g[4], h[4], k[4];
 };
 
+// FP32 (the MIXED form) takes the forward's Horner-form weights.
 template <typename T>
 SRT_HD void cr_weights4(T t, CRW4<T>& c) {
   CRW<T> b;
-  cr_weights(t, b);
+  if constexpr (sizeof(T) == sizeof(float))
+    cr_weights_mixed(t, b);
+  else
+    cr_weights(t, b);
   for (int i = 0; i < 4; ++i) {
     c.w[i] = b.w[i];
     c.g[i] = b.g[i];
@@ -614,8 +618,8 @@ SRT_HD void stage_view_mixed(const float* d, float s, const MixedRay& R, const G
     float th, tl;
     two_sum(x0[i], -p, th, tl);
     const float lo = (tl - pe) + d[i];
-    locate(th, lo, G.n[i], G.invn[i], cc[i], tc[i]);
-    locate(th - 0.5f, lo, G.n[i], G.invn[i], cs[i], ts[i]);
+    float df;
+    locate_mixed(th, lo, G.n[i], G.invn[i], cc[i], tc[i], cs[i], ts[i], df);
   }
   for (int f = 0; f < 4; ++f) {
     int cell[3];
