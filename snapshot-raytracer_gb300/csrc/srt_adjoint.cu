@@ -226,7 +226,7 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
   // flattened (step, stage) index, descending; u holds the stage inputs of q
   int q = (s1 - s0) * 4 - 1;
   float u[19];
-  for (int j = 0; j < 19; ++j) u[j] = tape[((int64_t)(q >> 2) * kTapeStep + 19 * (q & 3) + j) * A.count];
+  for (int j = 0; j < 19; ++j) u[j] = ld_stream(tape + ((int64_t)(q >> 2) * kTapeStep + 19 * (q & 3) + j) * A.count);
   float an[19];  // a of the stage after this one
 #pragma unroll 1
   for (; q >= 0; --q) {
@@ -244,7 +244,7 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
     stage_view_mixed(u, (float)st + c, R, A.G, x0, V);
     if (q > 0) {  // prefetch the next (earlier) stage's inputs
       const int qn = q - 1;
-      for (int j = 0; j < 19; ++j) u[j] = tape[((int64_t)(qn >> 2) * kTapeStep + 19 * (qn & 3) + j) * A.count];
+      for (int j = 0; j < 19; ++j) u[j] = ld_stream(tape + ((int64_t)(qn >> 2) * kTapeStep + 19 * (qn & 3) + j) * A.count);
     }
     for (int j = 0; j < 19; ++j) an[j] = 0.f;
     rhs_vjp<float, Acc, PAIR>(V, A.F, A.G, fb, an, acc);

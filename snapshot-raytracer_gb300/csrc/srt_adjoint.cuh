@@ -58,9 +58,11 @@ SRT_HD void cr_weights4(T t, CRW4<T>& c) {
 //   AccF64    FP64 atomics into a halo-padded grid (one per tap);
 //   AccFixed  64-bit fixed point into a halo-padded grid (order-independent,
 //             so repeated runs give identical bits).
-// A null grid (gradient not requested) ignores the contributions.
+// A null grid (gradient not requested) ignores the contributions, and the
+// passes skip forming them (active() is false).
 struct AccF32 {
   float4* g;
+  SRT_HD bool active() const { return g != nullptr; }
   SRT_HD void add_row(int64_t row, float c0, float c1, float c2, float c3) const {
     if (!g) return;
 #if defined(__CUDA_ARCH__)
@@ -76,6 +78,7 @@ struct AccF32 {
 
 struct AccF64 {
   double* g;
+  SRT_HD bool active() const { return g != nullptr; }
   SRT_HD void add(int64_t i, double v) const {
 #if defined(__CUDA_ARCH__)
     atomicAdd(g + i, v);
@@ -100,6 +103,7 @@ constexpr double kFixedScale = 4294967296.0;
 
 struct AccFixed {
   unsigned long long* g;
+  SRT_HD bool active() const { return g != nullptr; }
   SRT_HD void add(int64_t i, double v) const {
     const long long q = llrint(v * kFixedScale);
 #if defined(__CUDA_ARCH__)
@@ -132,6 +136,7 @@ SRT_HD void tricubic_vjp(const float* __restrict__ f, int64_t base, int64_t px, 
   cr_weights4(tx, X);
   cr_weights4(ty, Y);
   cr_weights4(tz, Z);
+  const bool scatter = acc.active();  // this field's gradient was requested
   // per-row scatter factors: the tap cotangent of row (b, c) is
   // wx_i Cw + gx_i Cg + hx_i Ch with Cw = wz_c Aw_b + gz_c Bw_b + hz_c Dw_b,
   // Cg = wz_c Ag_b + gz_c Bg_b, Ch = wz_c Ah_b.
@@ -169,11 +174,13 @@ SRT_HD void tricubic_vjp(const float* __restrict__ f, int64_t base, int64_t px, 
       s20 += Y.w[b] * r2;
       s21 += Y.g[b] * r2;
       s30 += Y.w[b] * r3;
-      const T Cw = Z.w[c] * Aw[b] + Z.g[c] * Bw[b] + Z.h[c] * Dw[b];
-      const T Cg = Z.w[c] * Ag[b] + Z.g[c] * Bg[b];
-      const T Ch = Z.w[c] * Ah[b];
-      acc.add_row(row, X.w[0] * Cw + X.g[0] * Cg + X.h[0] * Ch, X.w[1] * Cw + X.g[1] * Cg + X.h[1] * Ch,
-                  X.w[2] * Cw + X.g[2] * Cg + X.h[2] * Ch, X.w[3] * Cw + X.g[3] * Cg + X.h[3] * Ch);
+      if (scatter) {
+        const T Cw = Z.w[c] * Aw[b] + Z.g[c] * Bw[b] + Z.h[c] * Dw[b];
+        const T Cg = Z.w[c] * Ag[b] + Z.g[c] * Bg[b];
+        const T Ch = Z.w[c] * Ah[b];
+        acc.add_row(row, X.w[0] * Cw + X.g[0] * Cg + X.h[0] * Ch, X.w[1] * Cw + X.g[1] * Cg + X.h[1] * Ch,
+                    X.w[2] * Cw + X.g[2] * Cg + X.h[2] * Ch, X.w[3] * Cw + X.g[3] * Cg + X.h[3] * Ch);
+      }
     }
     const T zw = Z.w[c], zg = Z.g[c], zh = Z.h[c], zk = Z.k[c];
     o000 += zw * s00; o001 += zg * s00; o002 += zh * s00; o003 += zk * s00;
@@ -225,6 +232,7 @@ SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64
     xg[i] = dup2(X.g[i]);
     xh[i] = dup2(X.h[i]);
   }
+  const bool scatter = acc.active();  // this field's gradient was requested
   // y weights and per-row scatter factors of rows (0, 1) and (2, 3)
   float2 yw[2], yg[2], yh[2], yk[2], Aw[2], Bw[2], Dw[2], Ag[2], Bg[2], Ah[2];
   for (int pr = 0; pr < 2; ++pr) {
@@ -243,14 +251,28 @@ SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64
   float o000 = 0, o001 = 0, o002 = 0, o003 = 0, o010 = 0, o011 = 0, o012 = 0, o020 = 0, o021 = 0, o030 = 0;
   float o100 = 0, o101 = 0, o102 = 0, o110 = 0, o111 = 0, o120 = 0, o200 = 0, o201 = 0, o210 = 0, o300 = 0;
   const float2 z0 = make_float2(0.f, 0.f);
+  // taps of the next slice, loaded while the current one is processed
+  float2 nt[8];
+  for (int pr = 0; pr < 2; ++pr)
+    for (int i = 0; i < 4; ++i) nt[4 * pr + i] = ldg(f + basep + 2 * pr * px + i);
 #pragma unroll 1
   for (int c = 0; c < 4; ++c) {
     float2 s00 = z0, s01 = z0, s02 = z0, s03 = z0, s10 = z0, s11 = z0, s12 = z0, s20 = z0, s21 = z0, s30 = z0;
-    const float2 zw = dup2(Z.w[c]), zg = dup2(Z.g[c]), zh = dup2(Z.h[c]);
+    // this slice's z weights by selection (an indexed read of Z would put
+    // it in local memory)
+    const float zwc = c == 0 ? Z.w[0] : (c == 1 ? Z.w[1] : (c == 2 ? Z.w[2] : Z.w[3]));
+    const float zgc = c == 0 ? Z.g[0] : (c == 1 ? Z.g[1] : (c == 2 ? Z.g[2] : Z.g[3]));
+    const float zhc = c == 0 ? Z.h[0] : (c == 1 ? Z.h[1] : (c == 2 ? Z.h[2] : Z.h[3]));
+    const float zkc = c == 0 ? Z.k[0] : (c == 1 ? Z.k[1] : (c == 2 ? Z.k[2] : Z.k[3]));
+    const float2 zw = dup2(zwc), zg = dup2(zgc), zh = dup2(zhc);
+    float2 ct[8];
+    for (int i = 0; i < 8; ++i) ct[i] = nt[i];
+    if (c < 3)
+      for (int pr = 0; pr < 2; ++pr)
+        for (int i = 0; i < 4; ++i) nt[4 * pr + i] = ldg(f + basep + (c + 1) * pxy2 + 2 * pr * px + i);
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
-      const float2* rp = f + basep + c * pxy2 + 2 * pr * px;
-      const float2 t0 = ldg(rp), t1 = ldg(rp + 1), t2 = ldg(rp + 2), t3 = ldg(rp + 3);
+      const float2 t0 = ct[4 * pr], t1 = ct[4 * pr + 1], t2 = ct[4 * pr + 2], t3 = ct[4 * pr + 3];
       float2 r0 = fmul2(xw[0], t0), r1 = fmul2(xg[0], t0), r2 = fmul2(xh[0], t0), r3 = fmul2(dup2(X.k[0]), t0);
       r0 = ffma2(xw[1], t1, r0);
       r1 = ffma2(xg[1], t1, r1);
@@ -274,17 +296,17 @@ SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64
       s20 = ffma2(yw[pr], r2, s20);
       s21 = ffma2(yg[pr], r2, s21);
       s30 = ffma2(yw[pr], r3, s30);
-      // tap cotangents of the two rows
-      const float2 Cw = ffma2(zw, Aw[pr], ffma2(zg, Bw[pr], fmul2(zh, Dw[pr])));
-      const float2 Cg = ffma2(zw, Ag[pr], fmul2(zg, Bg[pr]));
-      const float2 Ch = fmul2(zw, Ah[pr]);
-      float2 v[4];
-      for (int i = 0; i < 4; ++i) v[i] = ffma2(xw[i], Cw, ffma2(xg[i], Cg, fmul2(xh[i], Ch)));
-      const int64_t row = base + c * pxy + 2 * pr * px;
-      acc.add_row(row, v[0].x, v[1].x, v[2].x, v[3].x);
-      acc.add_row(row + px, v[0].y, v[1].y, v[2].y, v[3].y);
+      if (scatter) {  // tap cotangents of the two rows
+        const float2 Cw = ffma2(zw, Aw[pr], ffma2(zg, Bw[pr], fmul2(zh, Dw[pr])));
+        const float2 Cg = ffma2(zw, Ag[pr], fmul2(zg, Bg[pr]));
+        const float2 Ch = fmul2(zw, Ah[pr]);
+        float2 v[4];
+        for (int i = 0; i < 4; ++i) v[i] = ffma2(xw[i], Cw, ffma2(xg[i], Cg, fmul2(xh[i], Ch)));
+        const int64_t row = base + c * pxy + 2 * pr * px;
+        acc.add_row(row, v[0].x, v[1].x, v[2].x, v[3].x);
+        acc.add_row(row + px, v[0].y, v[1].y, v[2].y, v[3].y);
+      }
     }
-    const float zwc = Z.w[c], zgc = Z.g[c], zhc = Z.h[c], zkc = Z.k[c];
     const float S00 = s00.x + s00.y, S01 = s01.x + s01.y, S02 = s02.x + s02.y, S03 = s03.x + s03.y;
     const float S10 = s10.x + s10.y, S11 = s11.x + s11.y, S12 = s12.x + s12.y;
     const float S20 = s20.x + s20.y, S21 = s21.x + s21.y, S30 = s30.x + s30.y;

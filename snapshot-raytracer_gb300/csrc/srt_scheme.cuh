@@ -49,9 +49,15 @@ enum { kFP64 = 0, kMIXED = 1, kREF16 = 2, kMIXED_PAIR = 3 };
 #if defined(__CUDA_ARCH__)
 template <typename T>
 SRT_HD T ldg(const T* p) { return __ldg(p); }
+// Streaming (evict-first) store and load for data touched once per pass (the
+// adjoint's tape), so it does not displace field taps from L1.
+SRT_HD void st_stream(float* p, float v) { __stcs(p, v); }
+SRT_HD float ld_stream(const float* p) { return __ldcs(p); }
 #else
 template <typename T>
 SRT_HD T ldg(const T* p) { return *p; }
+SRT_HD void st_stream(float* p, float v) { *p = v; }
+SRT_HD float ld_stream(const float* p) { return *p; }
 #endif
 
 // Halo-padded periodic grid: voxel (i,j,k), -1 <= i <= n0+1 (etc.), lives at
@@ -973,7 +979,7 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
     const float c = (st == 0) ? 0.f : ((st == 3) ? 1.f : 0.5f);
     mixed_stage(y, k, c, ys);
     if (us)
-      for (int j = 0; j < 19; ++j) us[(19 * st + j) * stride] = ys[j];
+      for (int j = 0; j < 19; ++j) st_stream(us + (19 * st + j) * stride, ys[j]);
     rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k, gd);
     // at s = 0 the ray sits exactly on the observer (a grid node, offsets
     // exactly 0) in both precisions, so no cell choice can differ there
