@@ -75,6 +75,8 @@ def parse():
     ap.add_argument("--oracle-sample", type=int, default=24, help="pixels checked against the FP64 oracle")
     ap.add_argument("--adjoint", default="256,128,128,12",
                     help="adjoint leg: grid,nside,n_steps,ckpt_every[,phi] ('' to skip; phi: w.r.t. phi only)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the adjoint leg and print its JSON object (a diagnostic, not the bench line)")
     return ap.parse_args()
 
 
@@ -322,6 +324,10 @@ def run_ours(args):
 
     import srt
     import srt_fields
+
+    if args.adjoint_only:
+        print(json.dumps({"adjoint": run_adjoint_leg(args.adjoint, args.seed, torch.device("cuda", 0))}), flush=True)
+        return
 
     rank, world, local = dist_setup(args.gpus)
     dev = torch.device("cuda", local)

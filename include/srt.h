@@ -140,6 +140,16 @@ int64_t srt_fields_bytes(const srt_fields* fields);
  * counterpart in the reference. */
 int srt_release_cached_memory(void);
 
+/* Failure injection for tests: after `after` more device allocations by this
+ * library have succeeded, the next one fails as if the device were out of
+ * memory (the call making it returns SRT_ERR_OUT_OF_MEMORY, frees what it had
+ * allocated and leaves earlier handles usable); the hook then disarms itself.
+ * after < 0 disarms it. Process-wide, for all devices and threads. The
+ * reference reports a failed cudaMalloc and returns -1
+ * (snapshot-raytracer.cu:752-772); this lets tests drive that path without
+ * exhausting a device. */
+int srt_debug_fail_alloc(int64_t after);
+
 /* -------------------------------------------------------------- forward */
 
 /* Trace one ray per HEALPix RING pixel p in [pix_begin, pix_begin+pix_count)

@@ -450,7 +450,7 @@ struct DevBuf {
   ~DevBuf() {
     if (p) cudaFree(p);
   }
-  cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 1); }
+  cudaError_t alloc(size_t bytes) { return dev_alloc(&p, bytes); }
 };
 
 template <typename Acc, typename E>
@@ -533,6 +533,7 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
 extern "C" int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
                        int precision, const float* const weights[SRT_NUM_MAPS], float* dphi, float* db_xyz,
                        int ckpt_every, unsigned flags, void* stream, srt_stats* stats) {
+  NvtxRange nvtx_("srt_vjp");
   return vjp_impl(fields, nside, pix_begin, pix_count, n_steps, precision, weights, dphi, db_xyz, ckpt_every, flags,
                   stream, stats, nullptr);
 }
@@ -765,6 +766,7 @@ done:
 extern "C" int srt_forward_tape(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
                                 int n_steps, int ckpt_every, float* const maps[SRT_NUM_MAPS], unsigned flags,
                                 void* stream, srt_stats* stats, srt_tape** out) {
+  NvtxRange nvtx_("srt_forward_tape");
   const auto t_wall = std::chrono::steady_clock::now();
   if (!out) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_tape: out is NULL");
   *out = nullptr;
@@ -895,6 +897,7 @@ done:
 
 extern "C" int srt_vjp_tape(const srt_tape* tape, const float* const weights[SRT_NUM_MAPS], float* dphi,
                             float* db_xyz, unsigned flags, void* stream, srt_stats* stats) {
+  NvtxRange nvtx_("srt_vjp_tape");
   if (!tape) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_vjp_tape: tape is NULL");
   return vjp_impl(tape->fields, tape->nside, tape->pix_begin, tape->pix_count, tape->n_steps, SRT_PRECISION_MIXED,
                   weights, dphi, db_xyz, tape->C, flags, stream, stats, tape);

@@ -1,5 +1,6 @@
 // srt_api.cu — the C ABI of libsrt (declared in include/srt.h): field upload
 // and layout, the forward trace, HEALPix helpers and error reporting.
+#include <atomic>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -48,7 +49,30 @@ cudaError_t device_pool(int dev, cudaMemPool_t* out) {
 
 namespace srt {
 
+// Failure injection (srt_debug_fail_alloc): device allocations still to
+// succeed before one fails; negative when disarmed.
+std::atomic<int64_t> g_alloc_fault_after{-1};
+
+// True for the allocation the hook makes fail (which disarms it).
+bool alloc_fault() {
+  int64_t v = g_alloc_fault_after.load();
+  while (v >= 0)
+    if (g_alloc_fault_after.compare_exchange_weak(v, v - 1)) return v == 0;
+  return false;
+}
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  if (alloc_fault()) return cudaErrorMemoryAllocation;
+  return cudaMalloc(p, bytes ? bytes : 1);
+}
+
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t s) {
+  if (alloc_fault()) return cudaErrorMemoryAllocation;
+  return cudaMallocAsync(p, bytes ? bytes : 1, s);
+}
+
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s) {
+  if (alloc_fault()) return cudaErrorMemoryAllocation;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   cudaMemPool_t pool = nullptr;
@@ -181,6 +205,7 @@ int srt_device_count(void) {
 
 int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t n1, int64_t n2,
                       unsigned flags, void* stream, srt_fields** out) {
+  NvtxRange nvtx_("srt_fields_create");
   if (!out) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_create: out is NULL");
   *out = nullptr;
   if (!phi || !b_xyz) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_create: phi and b_xyz are required");
@@ -219,6 +244,7 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
       if (kslab > n2) kslab = n2;
       SRT_CUDA_TRY(pool_alloc((void**)&slab, kslab * plane * 3 * sizeof(float), s), "allocate slab");
       // pass 0: phi (one component per voxel); pass 1: B (three, interleaved)
+      NvtxRange upload("upload and layout");
       for (int pass = 0; pass < 2; ++pass) {
         const int comps = pass == 0 ? 1 : 3;
         const float* src = pass == 0 ? phi : b_xyz;
@@ -266,6 +292,7 @@ fail:
 }
 
 int srt_fields_destroy(srt_fields* f) {
+  NvtxRange nvtx_("srt_fields_destroy");
   if (!f) return SRT_OK;
   int prev = 0;
   cudaGetDevice(&prev);
@@ -309,6 +336,7 @@ int64_t srt_fields_bytes(const srt_fields* f) { return f ? f->bytes : 0; }
 int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count, int n_steps,
                 int precision, float* const maps[SRT_NUM_MAPS], unsigned flags, void* stream,
                 srt_stats* stats) {
+  NvtxRange nvtx_("srt_forward");
   HostTimer wall;
   if (!fields) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward: fields is NULL");
   if (nside < 1 || nside > (int64_t(1) << 16))
@@ -378,8 +406,8 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     a.refine_count = nullptr;
     const bool refine = precision == SRT_PRECISION_MIXED && !(flags & SRT_MIXED_NO_REFINE);
     if (refine) {
-      SRT_CUDA_TRY(cudaMallocAsync((void**)&refine_list, pix_count * sizeof(int64_t), s), "cudaMallocAsync(refine list)");
-      SRT_CUDA_TRY(cudaMallocAsync((void**)&refine_count, sizeof(unsigned long long), s), "cudaMallocAsync(refine count)");
+      SRT_CUDA_TRY(dev_alloc_async((void**)&refine_list, pix_count * sizeof(int64_t), s), "cudaMallocAsync(refine list)");
+      SRT_CUDA_TRY(dev_alloc_async((void**)&refine_count, sizeof(unsigned long long), s), "cudaMallocAsync(refine count)");
       SRT_CUDA_TRY(cudaMemsetAsync(refine_count, 0, sizeof(unsigned long long), s), "clear refine count");
       a.refine_list = refine_list;
       a.refine_count = refine_count;
@@ -387,7 +415,7 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     if (dev_out) {
       for (int m = 0; m < 6; ++m) a.maps[m] = maps[m];
     } else {
-      SRT_CUDA_TRY(cudaMalloc(&dmaps, 6 * pix_count * sizeof(float)), "cudaMalloc(maps)");
+      SRT_CUDA_TRY(dev_alloc((void**)&dmaps, 6 * pix_count * sizeof(float)), "cudaMalloc(maps)");
       for (int m = 0; m < 6; ++m) a.maps[m] = dmaps + m * pix_count;
     }
     const bool timed = !(flags & SRT_ASYNC);
@@ -448,6 +476,11 @@ int64_t srt_nest2ring(int64_t nside, int64_t ipnest) {
 int64_t srt_ring2nest(int64_t nside, int64_t ipring) {
   if (!hp_is_pow2(nside) || nside > (int64_t(1) << 29) || ipring < 0 || ipring >= 12 * nside * nside) return -1;
   return hp_ring2nest(nside, ipring);
+}
+
+int srt_debug_fail_alloc(int64_t after) {
+  g_alloc_fault_after.store(after < 0 ? -1 : after);
+  return SRT_OK;
 }
 
 int srt_probe_peak(int kind, double* flops_per_s) {

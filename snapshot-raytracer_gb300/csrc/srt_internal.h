@@ -4,6 +4,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 #include <string>
+#include <nvtx3/nvToolsExt.h>
 #include "srt.h"
 #include "srt_scheme.cuh"
 
@@ -26,6 +27,20 @@ namespace srt {
 cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
 void pool_free(void* p, cudaStream_t s);
 int64_t pool_reusable_bytes(int dev);
+// cudaMalloc / cudaMallocAsync behind the failure-injection hook
+// (srt_debug_fail_alloc); pool_alloc checks the hook too.
+cudaError_t dev_alloc(void** p, size_t bytes);
+cudaError_t dev_alloc_async(void** p, size_t bytes, cudaStream_t s);
+
+// NVTX range over a scope (the public entry points and their phases), for
+// profilers' timelines and range filters; header-only, inert unless a tool
+// is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Error reporting (thread-local last error message).
 int set_error(int code, const char* fmt, ...);

@@ -94,6 +94,7 @@ def lib():
                                                  ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_int)]),
             "srt_free": (None, [_P]),
             "srt_release_cached_memory": (ctypes.c_int, []),
+            "srt_debug_fail_alloc": (ctypes.c_int, [_I64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
