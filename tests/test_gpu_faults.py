@@ -80,6 +80,39 @@ def test_vjp_allocation_failures(srt):
         assert np.all(np.isfinite(w_))
 
 
+def test_tape_pair_and_ref16_allocation_failures(srt):
+    import srt_fields
+
+    phi, b = srt_fields.int_noise_fields(20, seed=9)
+    nside, steps = 2, 12
+    w = np.random.default_rng(10).standard_normal((6, 12 * nside * nside)).astype(np.float32)
+    with srt.Fields(phi, b) as f:
+
+        def pair():
+            maps, tape, _ = f.forward_tape(nside, steps, ckpt_every=4)
+            try:
+                gphi, gb, _ = tape.vjp(w, deterministic=True)
+            finally:
+                tape.close()
+            return maps, gphi, gb
+
+        want = pair()
+        failed, got = _sweep_failures(srt, pair)
+        # tape: rays, checkpoints, re-trace list and counter, maps; vjp: its buffers
+        assert failed >= 5
+        for g, w_ in zip(got, want):
+            np.testing.assert_array_equal(g, w_)
+
+    # REF16 makes its FP16 planes on first use: a failure there leaves the
+    # handle usable and the next call makes them
+    with srt.Fields(phi, b) as f:
+        want16, _ = f.forward(nside, steps, precision="ref16")
+    with srt.Fields(phi, b) as f:
+        failed, got16 = _sweep_failures(srt, lambda: f.forward(nside, steps, precision="ref16")[0])
+        assert failed >= 1
+        np.testing.assert_array_equal(got16, want16)
+
+
 def test_hook_disarms_itself(srt):
     import srt_fields
 
