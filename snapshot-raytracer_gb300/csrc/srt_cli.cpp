@@ -28,6 +28,13 @@
 //                                 extent (n0 = dims[2], n2 = dims[0]), which
 //                                 keeps non-cubic grids consistent; by default
 //                                 n0 = dims[0], as the reference does
+//   --rescale-phi F, --rescale-b F
+//                                 multiply the potential / the B field by F
+//                                 after loading, with the reference's message
+//                                 (its compile-time RESCALE_DATA / RESCALE_BDATA,
+//                                 snapshot-raytracer.cu:663-670, :681-688):
+//                                 each value is multiplied in double and
+//                                 rounded back to float
 //
 // The six maps are written by six threads at once.
 //
@@ -63,6 +70,32 @@ bool parse_i64(const char* s, int64_t* v) {
   return true;
 }
 
+bool parse_f64(const char* s, double* v) {
+  char* end = nullptr;
+  errno = 0;
+  const double x = strtod(s, &end);
+  if (end == s || *end != '\0' || errno != 0 || !(x - x == 0.0)) return false;
+  *v = x;
+  return true;
+}
+
+// data[i] = float(data[i] * factor) over count values, on all host threads.
+void rescale(float* data, int64_t count, double factor) {
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  if (count < (int64_t(1) << 20)) nt = 1;
+  std::vector<std::thread> pool;
+  const int64_t chunk = (count + nt - 1) / nt;
+  for (unsigned t = 0; t < nt; ++t) {
+    const int64_t lo = t * chunk, hi = lo + chunk < count ? lo + chunk : count;
+    if (lo >= hi) break;
+    pool.emplace_back([=] {
+      for (int64_t i = lo; i < hi; ++i) data[i] = (float)((double)data[i] * factor);
+    });
+  }
+  for (auto& th : pool) th.join();
+}
+
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -75,7 +108,7 @@ void usage(const char* prog) {
   std::cerr << "  <n_steps>: Number of integration steps for raytracing (1 step = 1 grid unit)" << std::endl;
   std::cerr << "  [<batch>]: Optional batch index for processing a subset of pixels" << std::endl;
   std::cerr << "  options: [--precision mixed|fp64|ref16] [--overwrite] [--outdir DIR] [--timing] [--base-pixel]"
-               " [--xyz-order reference|hdf5]" << std::endl;
+               " [--xyz-order reference|hdf5] [--rescale-phi F] [--rescale-b F]" << std::endl;
 }
 
 }  // namespace
@@ -84,6 +117,8 @@ int main(int argc, char* argv[]) {
   std::vector<const char*> pos;
   int precision = SRT_PRECISION_MIXED;
   bool overwrite = false, timing = false, base_pixel = false, hdf5_order = false;
+  bool rescale_phi = false, rescale_b = false;
+  double phi_factor = 1.0, b_factor = 1.0;
   std::string outdir;
   if (const char* e = getenv("SRT_PRECISION")) {
     if (!strcmp(e, "fp64")) precision = SRT_PRECISION_FP64;
@@ -107,6 +142,16 @@ int main(int argc, char* argv[]) {
       outdir = argv[++i];
     } else if (!strcmp(argv[i], "--base-pixel")) {
       base_pixel = true;
+    } else if ((!strcmp(argv[i], "--rescale-phi") || !strcmp(argv[i], "--rescale-b")) && i + 1 < argc) {
+      const bool is_phi = !strcmp(argv[i], "--rescale-phi");
+      const char* v = argv[++i];
+      double x = 0.0;
+      if (!parse_f64(v, &x)) {
+        std::cerr << "Invalid rescaling factor: " << v << std::endl;
+        return -1;
+      }
+      (is_phi ? phi_factor : b_factor) = x;
+      (is_phi ? rescale_phi : rescale_b) = true;
     } else if (!strcmp(argv[i], "--xyz-order") && i + 1 < argc) {
       const char* o = argv[++i];
       if (!strcmp(o, "hdf5")) hdf5_order = true;
@@ -170,6 +215,12 @@ int main(int argc, char* argv[]) {
     return -1;
   }
   std::cout << "Data dimensions: " << dims[0] << " x " << dims[1] << " x " << dims[2] << std::endl;
+  if (rescale_phi) {
+    std::cout << "Rescaling potential data by factor " << phi_factor << std::endl;
+    int64_t count = 1;
+    for (int d = 0; d < rank; ++d) count *= dims[d];
+    rescale(phi, count, phi_factor);
+  }
   const double t_phi = now_ms();
 
   std::cout << "Loading B field data from HDF5 file " << pos[1] << " ..." << std::endl;
@@ -186,6 +237,16 @@ int main(int argc, char* argv[]) {
     srt_free(phi);
     srt_free(bxyz);
     return -1;
+  }
+  {
+    // the reference's size warning for a large B (snapshot-raytracer.cu:159-161)
+    const double b_bytes = 3.0 * (double)bdims[0] * (double)bdims[1] * (double)bdims[2] * sizeof(float);
+    if (b_bytes > 8.0 * 1024 * 1024 * 1024)
+      std::cerr << "Warning: allocating ~" << b_bytes / (1024.0 * 1024 * 1024) << " GiB for vector field." << std::endl;
+  }
+  if (rescale_b) {
+    std::cout << "Rescaling B field data by factor " << b_factor << std::endl;
+    rescale(bxyz, 3 * bdims[0] * bdims[1] * bdims[2], b_factor);
   }
   const double t_b = now_ms();
 

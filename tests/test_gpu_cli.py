@@ -44,6 +44,26 @@ def test_cli_maps_match_library(srt, tmp_path, batch):
         assert np.array_equal(got.view(np.uint32), ref[m].view(np.uint32)), name
 
 
+def test_cli_rescale_options(srt, tmp_path):
+    """--rescale-phi / --rescale-b: the runtime form of the reference's
+    RESCALE_DATA / RESCALE_BDATA (snapshot-raytracer.cu:663-670, :681-688),
+    with its messages after each field is loaded."""
+    phi, b = srt_fields.gaussian_fields_np(24, seed=7)
+    pp, pb = write_inputs(srt, tmp_path, phi, b)
+    nside, steps = 4, 12
+    r = subprocess.run([CLI, pp, pb, str(nside), str(steps), "--precision", "fp64", "--rescale-phi", "2",
+                        "--rescale-b", "0.25"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[3:7] == ["Data dimensions: 24 x 24 x 24", "Rescaling potential data by factor 2",
+                          "Loading B field data from HDF5 file %s ..." % pb, "Rescaling B field data by factor 0.25"]
+    ref = srt.trace((phi.astype(np.float64) * 2).astype(np.float32), (b.astype(np.float64) * 0.25).astype(np.float32),
+                    nside, steps, precision="fp64")
+    for m, name in enumerate(NAMES):
+        got = srt.fits_read_map(str(tmp_path / ("%s_batch0.fits" % name)))[0]
+        assert np.array_equal(got.view(np.uint32), ref[m].view(np.uint32)), name
+
+
 def test_cli_ref16_reproduces_reference_golden(srt, golden, tmp_path):
     meta, maps = golden
     case = "batch5_cube32_ns4_s16"

@@ -112,6 +112,11 @@ def test_cli_usage_and_argument_errors(tmp_path):
     assert r.returncode == 255 and "Invalid batch value: -1" in r.stderr
     r = run_cli("a.h5", "b.h5", "four", "10")
     assert r.returncode == 255 and "Invalid Nside value" in r.stderr
+    for bad in ("abc", "inf", "nan", "2x"):
+        r = run_cli("a.h5", "b.h5", "4", "10", "--rescale-phi", bad)
+        assert r.returncode == 255 and "Invalid rescaling factor: %s" % bad in r.stderr
+    r = run_cli("a.h5", "b.h5", "4", "10", "--rescale-b", "")
+    assert r.returncode == 255 and "Invalid rescaling factor" in r.stderr
     r = run_cli(tmp_path / "missing.h5", "b.h5", "4", "10")
     assert r.returncode == 255
     assert r.stdout.splitlines()[:3] == ["Nside: 4", "n_steps: 10",
