@@ -18,7 +18,10 @@ Also reported on the same line:
                form on one batch of the same workload, the mixed/FP64 speed
                ratio, and per-map errors of the mixed form against FP64;
   cpu_baseline the FP64 CPU oracle timed on a bounded sample of rays of the
-               same workload on all host cores.
+               same workload on all host cores;
+  adjoint      the mixed vjp against the mixed forward (--adjoint grid,nside,
+               n_steps,C[,phi]); --adjoint-only runs this leg alone and prints
+               its JSON object (a diagnostic, not the bench line).
 --impl reference times the reference's own CPU arithmetic for the path on the
 host cores (oracle/_ref where it was built from the reference sources, else
 the oracle's REF16 port) on bounded samples of the same workload, and adds
