@@ -692,19 +692,29 @@ SRT_HD void two_sum(float a, float b, float& s, float& e) {
 // floats; x is their exact sum), on the centred grid (faces at integers) and
 // on the grid staggered by -1/2 (faces at half-integers), and x's distance
 // from the nearest face of either grid. Every decision and the distance are
-// taken from an exact split of x: with fl = floor(th) and s + e = (th - fl) +
-// lo (two-sum), the fraction of x is u + e, u = s - floor(s) exact, so
-// frac(x) - 1/2 = (u - 1/2) + e carries its exact sign. tc / ts: offsets from
+// taken from a split of x that is exact up to the rounding of a remainder far
+// below the cell-face guard: with fl = floor(th), s + e = (th - fl) + lo
+// (two-sum) and u = s - floor(s), the fraction of x is u + e, where e also
+// holds the rounding errors of th - fl and of u (nonzero only when th or s
+// lies in (-1/2, 0)), so frac(x) - 1/2 = (u - 1/2) + e carries its exact sign. tc / ts: offsets from
 // the cells' lower faces (rounded; tc may round to 1 within ~3e-8 of the upper
 // face). dface: min(frac, 1 - frac, |frac - 1/2|), each with one rounding.
 SRT_HD void locate_mixed(float th, float lo, int n, float invn, int& cc, float& tc, int& cs, float& ts,
                          float& dface) {
   const float fl = floorf(th);
+  // th - fl is exact unless -1/2 < th < 0 (then fl = -1 and th + 1 rounds);
+  // b is its rounding error (exact: a + fl is exact whenever a was rounded)
+  const float a = th - fl;
+  const float b = th - (a + fl);
   float s, e;
-  two_sum(th - fl, lo, s, e);
+  two_sum(a, lo, s, e);
+  e += b;  // rounded, but with the sign of the exact remainder
   float k = floorf(s);
   if (s == k && e < 0.f) k -= 1.f;  // frac(x) = 1 + e: the cell below
-  const float u = s - k;            // exact, in [0, 1]
+  // u = s - k in [0, 1], exact unless -1/2 < s < 0 (lo took x below the
+  // face under th); its rounding error goes to e the same way
+  const float u = s - k;
+  e += s - (u + k);
   tc = u + e;
   const float v = (u - 0.5f) + e;   // frac(x) - 1/2 (u - 1/2 exact for u >= 1/4)
   const int c = (int)fl + (int)k;
