@@ -53,3 +53,41 @@ def test_fields_create_validates_shapes(srt):
     buf = np.zeros(16, np.float32)
     assert L.srt_fields_create(buf.ctypes.data, buf.ctypes.data, 0, 4, 4, 0, None, ctypes.byref(h)) == -1
     assert "bad grid extents" in srt.last_error()
+
+
+def test_plain_c_caller_links_and_runs(tmp_path):
+    """The header compiles as C99 and a C program links against libsrt the way
+    the reference's main() would call it: without a GPU the first call reports
+    SRT_ERR_NO_DEVICE with a message, and nothing exits."""
+    import subprocess
+
+    import build_srt
+
+    src = tmp_path / "use_srt.c"
+    src.write_text(r'''
+#include "srt.h"
+#include <stdio.h>
+int main(void) {
+  char msg[256];
+  srt_fields* F = NULL;
+  float phi[8] = {0}, b[24] = {0};
+  int rc = srt_fields_create(phi, b, 2, 2, 2, 0, NULL, &F);
+  srt_last_error(msg, sizeof msg);
+  printf("%d %d %s\n", srt_abi_version(), rc, msg);
+  if (rc == SRT_OK) srt_fields_destroy(F);
+  return 0;
+}
+''')
+    exe = tmp_path / "use_srt"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"), str(src),
+                        "-L" + build_srt.LIBDIR, "-lsrt", "-Wl,-rpath," + build_srt.LIBDIR, "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    ver, rc, msg = r.stdout.split(" ", 2)
+    assert int(ver) == 3
+    if has_gpu():
+        assert int(rc) == 0
+    else:
+        assert int(rc) == -6 and "no CUDA device" in msg
