@@ -60,7 +60,7 @@ def _nvcc_obj(src, verbose):
 def _gxx_obj(src, verbose):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     cuda_home = os.path.dirname(os.path.dirname(shutil.which(NVCC) or "/usr/local/cuda/bin/nvcc"))
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
            "-I" + os.path.join(cuda_home, "include"), "-c", src, "-o", obj]
     _run(cmd, verbose)
     return obj
@@ -106,7 +106,7 @@ def build(verbose=False, oracle=True, reference=True):
         if reference:
             side.append(ex.submit(build_reference, verbose))
         objs = [j.result() for j in jobs]
-        _run([NVCC, *GENCODE, "-shared", "-o", LIBSRT, *objs], verbose)
+        _run([NVCC, *GENCODE, "-shared", "-o", LIBSRT, *objs, "-lpthread"], verbose)
         cli_src = os.path.join(CSRC, "srt_cli.cpp")
         if os.path.isfile(cli_src):
             _run(["g++", "-O2", "-std=c++17", "-Wall", "-pthread", "-I" + os.path.join(ROOT, "include"), cli_src,

@@ -16,14 +16,20 @@
 // layouts v1-v4 (compact, contiguous, chunked with a v1 B-tree index, or v4's
 // single-chunk / implicit index); filters: deflate (zlib, loaded at run time),
 // shuffle, fletcher32 (checksum skipped). Anything else is rejected with
-// SRT_ERR_UNSUPPORTED and a message.
+// SRT_ERR_UNSUPPORTED and a message. The chunks of a B-tree-indexed dataset
+// are read (pread) and unfiltered on all host threads.
 #include <dlfcn.h>
+#include <unistd.h>
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 #include <sys/stat.h>
 #include "srt.h"
@@ -54,6 +60,20 @@ struct File {
     if (off > size || n > size - off) return false;
     if (fseeko(f, (off_t)off, SEEK_SET) != 0) return false;
     return fread(dst, 1, n, f) == n;
+  }
+  // The same without the stream's shared position (pread), for threads.
+  bool read_at(uint64_t off, void* dst, uint64_t n) const {
+    if (off > size || n > size - off) return false;
+    const int fd = fileno(f);
+    uint8_t* d = (uint8_t*)dst;
+    while (n > 0) {
+      const ssize_t got = pread(fd, d, n, (off_t)off);
+      if (got <= 0) return false;
+      d += got;
+      off += (uint64_t)got;
+      n -= (uint64_t)got;
+    }
+    return true;
   }
 };
 
@@ -644,7 +664,15 @@ struct Reader {
       }
       return out;
     }
-    // v1 B-tree of chunks (node type 1)
+    // v1 B-tree of chunks (node type 1): collect the leaf chunks, then read
+    // and unfilter them on all host threads (each chunk lands in its own
+    // part of the output)
+    struct Leaf {
+      uint64_t addr;
+      uint32_t size, mask;
+      std::vector<uint64_t> origin;
+    };
+    std::vector<Leaf> leaves;
     std::vector<uint64_t> stack{d.addr};
     int guard = 0;
     while (!stack.empty() && d.addr != kUndef) {
@@ -668,11 +696,41 @@ struct Reader {
           stack.push_back(child);
           continue;
         }
-        std::vector<uint8_t> cb = unfilter(d, bytes(child, csz), mask, cbytes);
-        if (cb.size() < cbytes) cb.resize(cbytes, 0);
-        place(cb, origin);
+        leaves.push_back(Leaf{child, csz, mask, origin});
       }
     }
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt < 1) nt = 1;
+    nt = (unsigned)std::min<size_t>(nt, leaves.size() / 4 + 1);
+    std::atomic<size_t> next{0};
+    std::mutex err_mutex;
+    bool failed = false;
+    H5Error first{0, ""};
+    auto work = [&]() {
+      for (size_t i = next++; i < leaves.size(); i = next++) {
+        try {
+          const Leaf& L = leaves[i];
+          std::vector<uint8_t> raw(L.size);
+          if (L.size && !F.read_at(base + L.addr, raw.data(), L.size)) fail(SRT_ERR_FORMAT, "read past end of file");
+          std::vector<uint8_t> cb = unfilter(d, std::move(raw), L.mask, cbytes);
+          if (cb.size() < cbytes) cb.resize(cbytes, 0);
+          place(cb, L.origin);
+        } catch (const H5Error& e) {
+          std::lock_guard<std::mutex> lock(err_mutex);
+          if (!failed) first = e;
+          failed = true;
+          next = leaves.size();
+        }
+      }
+    };
+    if (nt <= 1) {
+      work();
+    } else {
+      std::vector<std::thread> pool;
+      for (unsigned t = 0; t < nt; ++t) pool.emplace_back(work);
+      for (auto& th : pool) th.join();
+    }
+    if (failed) throw first;
     return out;
   }
 };

@@ -158,6 +158,26 @@ def test_h5_reader_v2_chunked_variants(srt, tmp_path, dtype, filters):
     assert np.array_equal(got, a.astype(np.float64).astype(np.float32))
 
 
+def test_h5_reader_many_chunks_in_parallel_and_a_corrupt_chunk(srt, tmp_path):
+    """528 deflated chunks read and unfiltered on all host threads land in the
+    right places; a corrupt chunk in the middle is reported from whichever
+    thread met it, as an error status with a message."""
+    import h5_variants
+
+    a = np.random.default_rng(6).standard_normal((40, 36, 44)).astype(np.float32)
+    p = str(tmp_path / "many.h5")
+    h5_variants.write_v2_chunked(p, a, chunk=(5, 6, 4))
+    assert np.array_equal(srt.h5_read_scalar(p), a)
+    raw = bytearray(open(p, "rb").read())
+    mid = len(raw) // 3  # inside the chunk data, which follows the 48-byte superblock
+    raw[mid:mid + 64] = bytes(64)
+    q = str(tmp_path / "corrupt.h5")
+    open(q, "wb").write(bytes(raw))
+    with pytest.raises(srt.SrtError) as ei:
+        srt.h5_read_scalar(q)
+    assert "corrupt deflate chunk" in str(ei.value)
+
+
 def test_h5_reader_vector3_chunked(srt, tmp_path):
     import h5_variants
 
