@@ -110,3 +110,15 @@ def test_ray_positions_of_the_trace(loc):
             tl = float(Fraction(float(x0)) - Fraction(float(p)) - Fraction(float(th)))
             lo = np.float32(np.float32(tl - pe) + np.float32(dx))
             check(loc, th, lo, n)
+
+
+def test_far_outside_the_box(loc):
+    """Rays that wrapped around the periodic box many times: positions far
+    outside [0, n) still give the exact cells modulo n (every tap index stays
+    in range), through the integer wrap of the cell index."""
+    rng = np.random.default_rng(14)
+    for n in (16, 1000, 1024):
+        for _ in range(2000):
+            th = np.float32(rng.choice([-1.0, 1.0]) * 10.0 ** rng.uniform(1, 6.5))
+            lo = np.float32(rng.standard_normal() * 1e-3)
+            check(loc, th, lo, n)
