@@ -60,8 +60,11 @@ def _ohdr_v2(msgs):
     return b"OHDR" + bytes([2, 0x02]) + struct.pack("<I", len(body)) + body + b"\0\0\0\0"
 
 
-def write_v2_chunked(path, data, chunk, filters=("shuffle", "deflate"), array3=False):
-    """Superblock v2, v2 object headers, chunked + filtered dataset /data."""
+def write_v2_chunked(path, data, chunk, filters=("shuffle", "deflate"), array3=False, fanout=None):
+    """Superblock v2, v2 object headers, chunked + filtered dataset /data.
+    fanout: at most this many entries per v1 B-tree node, so that many chunks
+    give a tree of several levels (libhdf5 writes 2K = 64 per node by default);
+    None: one leaf node holding every chunk."""
     data = np.ascontiguousarray(data)
     shape = data.shape[:-1] if array3 else data.shape
     rank = len(shape)
@@ -94,16 +97,31 @@ def write_v2_chunked(path, data, chunk, filters=("shuffle", "deflate"), array3=F
         addr = f.here()
         f.put(raw)
         entries.append((origin, len(raw), addr))
-    # chunk B-tree (leaf)
-    f.pad()
-    btree = f.here()
-    f.put(b"TREE" + bytes([1, 0]) + struct.pack("<H", len(entries)))
-    f.u(UNDEF, 8)
-    f.u(UNDEF, 8)
-    for origin, size, addr in entries:
-        f.put(struct.pack("<II", size, 0) + b"".join(struct.pack("<Q", o) for o in origin + [0]))
-        f.u(addr, 8)
-    f.put(struct.pack("<II", 0, 0) + b"".join(struct.pack("<Q", s) for s in list(shape) + [0]))
+    # chunk B-tree: leaves of chunk entries, then parent levels of node entries
+    # (each entry: key = chunk size, filter mask and offsets of the first chunk
+    # below it; child address), each node closed by the key of its upper bound
+    def node(level, items, upper):
+        f.pad()
+        at = f.here()
+        f.put(b"TREE" + bytes([1, level]) + struct.pack("<H", len(items)))
+        f.u(UNDEF, 8)
+        f.u(UNDEF, 8)
+        for origin, size, addr in items:
+            f.put(struct.pack("<II", size, 0) + b"".join(struct.pack("<Q", o) for o in origin + [0]))
+            f.u(addr, 8)
+        f.put(struct.pack("<II", 0, 0) + b"".join(struct.pack("<Q", s) for s in upper + [0]))
+        return at
+
+    level, items = 0, entries
+    m = fanout or max(len(entries), 1)
+    while True:
+        groups = [items[i:i + m] for i in range(0, len(items), m)]
+        addrs = [node(level, g, list(shape)) for g in groups]
+        if len(groups) == 1:
+            btree = addrs[0]
+            break
+        items = [(g[0][0], g[0][1], a) for g, a in zip(groups, addrs)]
+        level += 1
     # dataset header
     space = struct.pack("<BBBB", 2, rank, 0, 1) + b"".join(struct.pack("<Q", s) for s in shape)
     layout = struct.pack("<BBB", 3, 2, rank + 1) + struct.pack("<Q", btree) + \

@@ -178,6 +178,22 @@ def test_h5_reader_many_chunks_in_parallel_and_a_corrupt_chunk(srt, tmp_path):
     assert "corrupt deflate chunk" in str(ei.value)
 
 
+@pytest.mark.parametrize("fanout", [64, 3])
+def test_h5_reader_multilevel_chunk_btree(srt, tmp_path, fanout):
+    """Chunk B-trees of several levels, as libhdf5 writes them for many chunks
+    (2K = 64 entries per node; fanout 3 gives five levels here)."""
+    import h5_variants
+
+    a = np.random.default_rng(8).standard_normal((24, 20, 28)).astype(np.float32)
+    p = str(tmp_path / ("ml%d.h5" % fanout))
+    h5_variants.write_v2_chunked(p, a, chunk=(4, 4, 4), fanout=fanout)  # 6 x 5 x 7 = 210 chunks
+    assert np.array_equal(srt.h5_read_scalar(p), a)
+    v = np.random.default_rng(9).standard_normal((9, 8, 10, 3)).astype(np.float32)
+    q = str(tmp_path / ("mlv%d.h5" % fanout))
+    h5_variants.write_v2_chunked(q, v, chunk=(2, 3, 4), array3=True, fanout=fanout)
+    assert np.array_equal(srt.h5_read_vector3(q), v)
+
+
 def test_h5_reader_vector3_chunked(srt, tmp_path):
     import h5_variants
 
