@@ -46,14 +46,21 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 # Algorithmic work of one RK4 step of one ray (4 right-hand-side evaluations,
-# each 4 tricubic interpolations with value, gradient and Hessian):
+# each with 4 tricubic interpolations of value, gradient and Hessian), counted
+# operation by operation from the scheme (snapshot-raytracer.cu:195-550) as
+# this build forms it, one FMA = 2 FLOP:
 #   tricubic, separable: x pass 16 rows x 3 outputs x 4 taps, y pass 4 x 6 x 4,
-#     z pass 10 x 4 multiply-adds = 328 FMA = 656 FLOP, plus 3 axes x 12
-#     Catmull-Rom weights (48 FLOP per axis) = 144 FLOP  -> 800 FLOP
-#   right-hand side outside the interpolations (unit vectors, projections, B
-#     tidal terms, Sachs equations)                         -> 330 FLOP
-#   RK4 stage states and accumulation, 19 components        -> 152 FLOP
-FLOP_PER_RAY_STEP = 4 * (4 * 800 + 330) + 152          # = 14,272
+#     z pass 10 x 4 multiply-adds = 328 FMA                     ->  656 FLOP
+#   Catmull-Rom weights of value, d/dt, d2/dt2 (Horner form, 38 FLOP a set):
+#     6 sets per right-hand side (3 centred axes shared by phi and by the two
+#     unstaggered axes of each B component, 3 staggered)        ->  228 FLOP
+#   right-hand side outside the interpolations: unit n, e1, e2 (27), the B
+#     sums n.grad B, e.n.grad B, tidal matrix, n.lap B (3 x 72), the geodesic,
+#     transport and Sachs terms with the dA > 1/2 branch (203)  ->  446 FLOP
+#   RK4 stage states (3 x 38), accumulation (76), update (57)   ->  247 FLOP
+# The packed z pass's idle half-lanes, the perturbation form's compensated
+# sums and the exact position split are implementation overhead, not counted.
+FLOP_PER_RAY_STEP = 4 * (4 * 656 + 228 + 446) + 247    # = 13,439
 # Bytes gathered per ray-step: 4 stages x 4 fields x 64 taps x 4 B (FP32 fields).
 GATHER_BYTES_PER_RAY_STEP = 4 * 4 * 64 * 4               # = 4,096
 MAP_NAMES = ("dA", "ellipticity1", "ellipticity2", "rotation", "deflection1", "deflection2")
@@ -75,7 +82,13 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--compare-batch", type=int, default=5, help="batch used for the FP64 / REF16 legs (-1: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
-    ap.add_argument("--oracle-sample", type=int, default=24, help="pixels checked against the FP64 oracle")
+    ap.add_argument("--oracle-sample", type=int, default=3072,
+                    help="pixels checked against the FP64 oracle (one run of consecutive pixels in each of the 12 "
+                         "batches)")
+    ap.add_argument("--parity", action="store_true",
+                    help="parity record of the workload instead of the bench line: full-sky MIXED, FP64 and REF16 "
+                         "forms, the reference's own GPU build batch by batch (all 12 batches), and the FP64 oracle "
+                         "on --oracle-sample pixels over all batches; prints one JSON object")
     ap.add_argument("--adjoint", default="256,128,128,12",
                     help="adjoint leg: grid,nside,n_steps,ckpt_every[,phi] ('' to skip; phi: w.r.t. phi only)")
     ap.add_argument("--adjoint-only", action="store_true",
@@ -189,6 +202,14 @@ def sample_pixels(nside, count, begin=0, total=None, seed=0):
     total = 12 * nside * nside - begin if total is None else total
     rng = np.random.default_rng(seed)
     return np.sort(rng.choice(total, size=min(count, total), replace=False)) + begin
+
+
+def batch_runs(nside, total, seed=0):
+    """One run of total // 12 consecutive RING pixels at a seeded offset in
+    each of the 12 batches [b nside^2, (b + 1) nside^2): [(begin, count)]."""
+    per = max(1, min(total // 12, nside * nside))
+    rng = np.random.default_rng(seed)
+    return [(b * nside * nside + int(rng.integers(0, nside * nside - per + 1)), per) for b in range(12)]
 
 
 def time_cpu(fn, target_s, make_sample, start=16):
@@ -320,6 +341,71 @@ def run_adjoint_leg(spec, seed, dev):
     return res
 
 
+# ------------------------------------------------------------ parity record
+
+def run_parity(args):
+    """Per-map errors of every form at one workload (all 12 batches): MIXED,
+    FP64 and REF16 full skies; the reference's own GPU build run batch by batch
+    as its CLI runs them (snapshot-raytracer.cu:708-717, :897-901) and the 12
+    batch maps summed into a sky; the FP64 oracle on a run of pixels in every
+    batch. Errors are relative to each map's rms signal (map_errors)."""
+    import torch
+
+    import srt
+    import srt_fields
+    from oracle import oracle
+
+    n, nside, S = args.n, args.nside, args.n_steps
+    npix = 12 * nside * nside
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    phi_d, b_d = srt_fields.gaussian_fields_torch(n, seed=args.seed, device=dev)
+    res = {"workload": "%d^3 fields, nside %d (%d rays, 12 batches), %d steps" % (n, nside, npix, S),
+           "fields": "gaussian P(k)~k^-3, phi rms 1e-5, transverse B rms 1e-7, torch generator seed %d" % args.seed}
+    maps, secs = {}, {}
+    with srt.Fields(phi_d, b_d) as f:
+        for mode in ("mixed", "fp64", "ref16"):
+            o = torch.empty((6, npix), dtype=torch.float32, device=dev)
+            f.forward(nside, S, precision=mode, out=o)  # REF16 builds its planes on first use
+            _, st = f.forward(nside, S, precision=mode, out=o)
+            torch.cuda.synchronize()
+            maps[mode] = o.cpu().numpy()
+            secs[mode] = {"kernel_ms": st.trace_ms, "ray_steps_per_s": npix * S / (st.trace_ms * 1e-3),
+                          "refined_rays": st.refined_rays}
+            del o
+    res["forms"] = secs
+    ref = None
+    if oracle.ref_gpu_available():
+        ref = np.zeros((6, npix), np.float32)
+        kms = 0.0
+        for bt in range(12):
+            r, ms = oracle.ref_gpu_trace(phi_d, b_d, nside, S, bt * nside * nside, nside * nside)
+            ref[:, bt * nside * nside:(bt + 1) * nside * nside] = r.cpu().numpy()
+            kms += ms[0]
+        res["reference_gpu_build"] = {"kernel_ms_12_batches": kms, "ray_steps_per_s": npix * S / (kms * 1e-3)}
+    phi_np, b_np = phi_d.cpu().numpy(), b_d.cpu().numpy()
+    del phi_d, b_d
+    torch.cuda.empty_cache()
+    ranges = batch_runs(nside, args.oracle_sample, seed=1)
+    pix = np.concatenate([np.arange(lo, lo + c) for lo, c in ranges])
+    t0 = time.perf_counter()
+    want = oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="fp64", threads=oracle.max_threads())
+    res["oracle_sample"] = {"pixels": len(pix), "runs": "%d runs of %d consecutive RING pixels, one per batch"
+                            % (len(ranges), ranges[0][1]), "cpu_s": time.perf_counter() - t0,
+                            "cores": oracle.max_threads()}
+    err = {}
+    for name in ("fp64", "mixed", "ref16"):
+        err["%s_vs_oracle" % name] = map_errors(maps[name][:, pix], want)
+    err["mixed_vs_fp64_full_sky"] = map_errors(maps["mixed"], maps["fp64"])
+    err["ref16_vs_fp64_full_sky"] = map_errors(maps["ref16"], maps["fp64"])
+    if ref is not None:
+        err["reference_build_vs_oracle"] = map_errors(ref[:, pix], want)
+        err["reference_build_vs_fp64_full_sky"] = map_errors(ref, maps["fp64"])
+        err["reference_build_vs_ref16_full_sky"] = map_errors(ref, maps["ref16"])
+    res["errors"] = err
+    print(json.dumps({"parity": res}), flush=True)
+
+
 # --------------------------------------------------------------- our arm
 
 def run_ours(args):
@@ -330,6 +416,9 @@ def run_ours(args):
 
     if args.adjoint_only:
         print(json.dumps({"adjoint": run_adjoint_leg(args.adjoint, args.seed, torch.device("cuda", 0))}), flush=True)
+        return
+    if args.parity:
+        run_parity(args)
         return
 
     rank, world, local = dist_setup(args.gpus)
@@ -467,11 +556,19 @@ def run_ours(args):
         if phi_np is not None and args.oracle_sample > 0:
             from oracle import oracle
 
-            pix = sample_pixels(nside, args.oracle_sample, b0, cnt, seed=1)
-            want = oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="fp64")
+            # a run of consecutive RING pixels in each of the 12 batches: the
+            # FP64 oracle on all of them, against the MIXED full sky of the
+            # timed region and the FP64 GPU form traced on the same runs
+            ranges = batch_runs(nside, args.oracle_sample, seed=1)
+            pix = np.concatenate([np.arange(lo, lo + c) for lo, c in ranges])
+            want = oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="fp64", threads=oracle.max_threads())
+            f64 = np.concatenate([fields.forward(nside, S, lo, c, precision="fp64")[0] for lo, c in ranges], axis=1)
+            mixed = out[:, torch.from_numpy(pix).to(dev)].cpu().numpy()
             cmp["oracle_sample"] = {"pixels": len(pix),
-                                    "fp64_gpu_vs_oracle": map_errors(maps["fp64"][:, pix - b0], want),
-                                    "mixed_gpu_vs_oracle": map_errors(maps["mixed"][:, pix - b0], want)}
+                                    "runs": "%d runs of %d consecutive RING pixels, one in each batch" %
+                                            (len(ranges), ranges[0][1]),
+                                    "fp64_gpu_vs_oracle": map_errors(f64, want),
+                                    "mixed_gpu_vs_oracle": map_errors(mixed, want)}
         result["compare"] = cmp
 
     # ---- adjoint leg (rank 0)

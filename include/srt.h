@@ -51,6 +51,8 @@ extern "C" {
 #define SRT_ERR_FORMAT (-5)
 #define SRT_ERR_NO_DEVICE (-6)
 #define SRT_ERR_UNSUPPORTED (-7)
+#define SRT_ERR_OVERFLOW (-8) /* srt_vjp, SRT_DETERMINISTIC: a gradient beyond the
+                                 fixed-point range */
 
 /* precision modes of srt_forward / srt_vjp */
 #define SRT_PRECISION_FP64 0  /* all-FP64 interpolation, right-hand side and state */
@@ -136,8 +138,10 @@ int64_t srt_fields_bytes(const srt_fields* fields);
 /* Field memory comes from a per-device pool that keeps what srt_fields_destroy
  * hands back, so that the next srt_fields_create of the same size is not slowed
  * down by the driver mapping tens of GB again. This returns the pool's unused
- * memory to the device (a failed allocation also does, before retrying). No
- * counterpart in the reference. */
+ * memory to the device (a failed allocation also does, before retrying), and
+ * forgets the device addresses srt_forward_noalloc looked up (call it after a
+ * cudaDeviceReset, before the next srt_forward_noalloc). No counterpart in the
+ * reference. */
 int srt_release_cached_memory(void);
 
 /* Failure injection for tests: after `after` more device allocations by this
@@ -190,7 +194,10 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
  * rejected with SRT_ERR_INVALID_ARGUMENT. The first call on a device looks up
  * the array's address (make it before any stream capture). Calls share the
  * array: calls whose work overlaps on the GPU race. Synchronous unless
- * SRT_ASYNC. No counterpart in the reference (it has no library API). */
+ * SRT_ASYNC; SRT_NESTED_RANGE and SRT_MIXED_NO_REFINE act as in srt_forward;
+ * any other flag (bar SRT_OUTPUT_DEVICE, which is implied) is refused with
+ * SRT_ERR_UNSUPPORTED. No counterpart in the reference (it has no library
+ * API). */
 int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
                         int n_steps, int precision, float* const maps[SRT_NUM_MAPS], unsigned flags,
                         void* stream);
@@ -204,7 +211,10 @@ int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int64_t pix_beg
  * state is checkpointed every ckpt_every steps (<= 0 picks ~sqrt(n_steps)) and
  * each segment is recomputed during the reverse sweep. Gradients are
  * overwritten unless SRT_ACCUMULATE. SRT_DETERMINISTIC accumulates in 64-bit
- * fixed point so repeated calls give identical bits.
+ * fixed point (2^32 units per unit of gradient) so repeated calls give
+ * identical bits; a voxel whose gradient, or a single contribution to it,
+ * reaches 2^30 in magnitude (or is not finite) makes the call fail with
+ * SRT_ERR_OVERFLOW instead of returning wrapped sums.
  * No counterpart in the reference (it has no derivatives); the forward it
  * differentiates is snapshot-raytracer.cu:315-583. */
 int srt_vjp(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,

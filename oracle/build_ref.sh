@@ -3,10 +3,16 @@
 # oracle/_ref/libsrt_ref.so (test infrastructure: golden vectors and the pin of
 # the oracle). Reads the reference sources where they lie; writes only into
 # oracle/_ref/. Usage: oracle/build_ref.sh [REFERENCE_DIR]
+# The reference directory is the argument, else $SRT_REFERENCE_DIR, else the
+# read-only mount this recipe was written for (/root/reference). Exit status 3
+# (and a message) when none of them holds snapshot-raytracer.cu.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${SRT_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
-[ -f "$REF/snapshot-raytracer.cu" ] || { echo "reference source not found in $REF" >&2; exit 3; }
+[ -f "$REF/snapshot-raytracer.cu" ] || {
+  echo "oracle/build_ref.sh: no reference sources in '$REF' (pass the directory holding snapshot-raytracer.cu or set SRT_REFERENCE_DIR); oracle/_ref not built" >&2
+  exit 3
+}
 mkdir -p "$HERE/_ref"
 # Reference flags (Makefile:9-10,33): -O3 --use_fast_math -std=c++17 -fopenmp;
 # one Blackwell gencode for its device code, which the library never launches.

@@ -21,7 +21,6 @@ LIBSRT = os.path.join(LIBDIR, "libsrt.so")
 CLI = os.path.join(PKG, "snapshot-raytracer")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 LIBORACLE = os.path.join(ORACLE_DIR, "liboracle.so")
-REFERENCE_DIR = os.environ.get("SRT_REFERENCE_DIR", "/root/reference")
 LIBREF = os.path.join(ORACLE_DIR, "_ref", "libsrt_ref.so")
 LIBREFGPU = os.path.join(ORACLE_DIR, "librefgpu.so")
 REFCUBIN = os.path.join(ORACLE_DIR, "_ref", "ref_kernel.cubin")
@@ -84,10 +83,20 @@ def build_oracle(verbose=False):
 
 
 def build_reference(verbose=False):
-    """The reference's own host code for the path (only where its sources exist)."""
-    if not os.path.isfile(os.path.join(REFERENCE_DIR, "snapshot-raytracer.cu")):
+    """The reference's own host code and device code for the path, compiled by
+    oracle/build_ref.sh from the reference sources (SRT_REFERENCE_DIR, or the
+    directory that recipe names); skipped, with the recipe's message, where the
+    sources are absent (e.g. on the GPU machine, which runs the files built here)."""
+    cmd = ["sh", os.path.join(ORACLE_DIR, "build_ref.sh")]
+    if os.environ.get("SRT_REFERENCE_DIR"):
+        cmd.append(os.environ["SRT_REFERENCE_DIR"])
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode == 3:  # the recipe found no reference sources
+        if verbose:
+            print(r.stdout.strip(), flush=True)
         return None
-    _run(["sh", os.path.join(ORACLE_DIR, "build_ref.sh"), REFERENCE_DIR], verbose)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed (%d): %s\n%s" % (r.returncode, " ".join(cmd), r.stdout))
     return LIBREF
 
 

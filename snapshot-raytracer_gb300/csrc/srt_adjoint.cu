@@ -409,7 +409,7 @@ struct PadRead<float4> {  // row-expanded FP32: taps of the rows starting at q, 
 // halo copies) -> out[v * stride + comp] (+= when accumulate).
 template <typename G>
 __global__ void fold_kernel(const G* __restrict__ padded, int64_t n0, int64_t n1, int64_t n2, float* out, int stride,
-                            int comp, int accumulate) {
+                            int comp, int accumulate, unsigned* ovf) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n0 * n1 * n2) return;
   const PadRead<G> rd{padded};
@@ -434,7 +434,9 @@ __global__ void fold_kernel(const G* __restrict__ padded, int64_t n0, int64_t n1
   for (int a = 0; a < nk; ++a)
     for (int b = 0; b < nj; ++b)
       for (int c = 0; c < ni; ++c) sum += rd(pi[c] + p0 * (pj[b] + p1 * pk[a]));
-  const float val = (float)PadRead<G>::value(sum);
+  const double dval = PadRead<G>::value(sum);
+  if (ovf && !(fabs(dval) < kFixedLimit)) atomicOr(ovf, 1u);  // fixed point near or past its range
+  const float val = (float)dval;
   float* dst = out + v * stride + comp;
   *dst = accumulate ? *dst + val : val;
 }
@@ -574,7 +576,7 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
   int prev = 0;
   cudaGetDevice(&prev);
   if (prev != f->device) cudaSetDevice(f->device);
-  DevBuf counts, offsets, rays, wdev, ckpt, seg, lam, gacc[4], gout_phi, gout_b;
+  DevBuf counts, offsets, rays, wdev, ckpt, seg, lam, gacc[4], gout_phi, gout_b, ovf;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   int64_t kernels = 0, h2d = 0, d2h = 0;
   {
@@ -636,6 +638,10 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
         VJP_TRY(gacc[fld].alloc(pvox * accsz), "cudaMalloc(gradient accumulators)");
         VJP_TRY(cudaMemsetAsync(gacc[fld].p, 0, pvox * accsz, s), "clear accumulators");
       }
+      if (determ) {  // fixed-point range flag
+        VJP_TRY(ovf.alloc(sizeof(unsigned)), "cudaMalloc(overflow flag)");
+        VJP_TRY(cudaMemsetAsync(ovf.p, 0, sizeof(unsigned), s), "clear overflow flag");
+      }
 
       AdjArgs A;
       A.F = make_ptrs(f);
@@ -664,6 +670,7 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
         if (determ) {
           AccFixed ac[4];
           make_acc<AccFixed, unsigned long long>(ac, A.acc);
+          for (int fld = 0; fld < 4; ++fld) ac[fld].ovf = (unsigned*)ovf.p;
           reverse_kernel_fp64<AccFixed><<<blocks, 128, 0, s>>>(A, ac[0], ac[1], ac[2], ac[3]);
         } else {
           AccF64 ac[4];
@@ -687,6 +694,7 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
         AccFixed ax[4];
         make_acc<AccF32, float4>(af, A.acc);
         make_acc<AccFixed, unsigned long long>(ax, A.acc);
+        for (int fld = 0; fld < 4; ++fld) ax[fld].ovf = (unsigned*)ovf.p;
         for (int sgi = nseg - 1; sgi >= 0; --sgi) {
           if (pair)
             segment_kernel_mixed<true><<<blocks, 128, 0, s>>>(A, sgi);
@@ -715,13 +723,14 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
         const int accum = accumulate ? 1 : 0;
         if (determ)
           fold_kernel<unsigned long long><<<fblocks, 256, 0, s>>>((const unsigned long long*)gacc[fld].p, f->n[0],
-                                                                 f->n[1], f->n[2], dst, stride, comp, accum);
+                                                                 f->n[1], f->n[2], dst, stride, comp, accum,
+                                                                 (unsigned*)ovf.p);
         else if (fp64)
           fold_kernel<double><<<fblocks, 256, 0, s>>>((const double*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
-                                                     stride, comp, accum);
+                                                     stride, comp, accum, nullptr);
         else
           fold_kernel<float4><<<fblocks, 256, 0, s>>>((const float4*)gacc[fld].p, f->n[0], f->n[1], f->n[2], dst,
-                                                     stride, comp, accum);
+                                                     stride, comp, accum, nullptr);
         ++kernels;
       }
       VJP_TRY(cudaGetLastError(), "fold kernel");
@@ -741,6 +750,16 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
       }
     }
     VJP_TRY(cudaStreamSynchronize(s), "srt_vjp");
+    if (ovf.p) {
+      unsigned flag = 0;
+      VJP_TRY(cudaMemcpy(&flag, ovf.p, sizeof(flag), cudaMemcpyDeviceToHost), "read overflow flag");
+      if (flag) {
+        rc = set_error(SRT_ERR_OVERFLOW,
+                       "srt_vjp: SRT_DETERMINISTIC gradient beyond the fixed-point range (|gradient| >= 2^30 per "
+                       "voxel, or not finite); the gradients are not valid (use the FP32/FP64 accumulation)");
+        goto done;
+      }
+    }
     if (stats) {
       float ms = -1.f;
       if (e0 && e1) cudaEventElapsedTime(&ms, e0, e1);

@@ -98,13 +98,26 @@ struct AccF64 {
 // Fixed point with kFixedScale = 2^32 units per unit of gradient; |gradient|
 // per voxel must stay below 2^31. Contributions are rounded to the nearest
 // unit before the integer addition, so the result does not depend on the
-// order of the additions.
+// order of the additions. A contribution of magnitude 2^30 or more (or one
+// that is not finite) sets *ovf, where the integer sum may already have
+// wrapped; the fold kernel sets it too for a folded |gradient| >= 2^30, and
+// srt_vjp then fails with SRT_ERR_OVERFLOW instead of returning wrapped values.
 constexpr double kFixedScale = 4294967296.0;
+constexpr double kFixedLimit = 1073741824.0;  // 2^30 units of gradient
 
 struct AccFixed {
   unsigned long long* g;
+  unsigned* ovf = nullptr;
   SRT_HD bool active() const { return g != nullptr; }
   SRT_HD void add(int64_t i, double v) const {
+    if (!(fabs(v) < kFixedLimit)) {
+#if defined(__CUDA_ARCH__)
+      if (ovf) atomicOr(ovf, 1u);
+#else
+      if (ovf) *ovf |= 1u;
+#endif
+      v = 0.0;  // llrint of it would be undefined
+    }
     const long long q = llrint(v * kFixedScale);
 #if defined(__CUDA_ARCH__)
     atomicAdd(g + i, (unsigned long long)q);
@@ -213,15 +226,14 @@ SRT_HD void tricubic_vjp(const float* __restrict__ f, int64_t base, int64_t px, 
            qb[6] * o102 + qb[7] * o021 + qb[8] * o012 + qb[9] * o003;
 }
 
-// The same pass on the row-pair array (FP32 only): rows y and y+1 of a slice
-// arrive in one 64-bit load per x tap and every product runs on packed pairs
-// (two FP32 FMAs per instruction), as in tricubic_pair. basep: pair index of
-// voxel (cx-1, cy-1, cz-1); base: its index in the single layout, where the
-// tap cotangents go.
-template <typename Acc>
-SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64_t base, int64_t px, int64_t pxy,
-                              int64_t pxy2, float tx, float ty, float tz, const float* qb, Tri<float>& Q, float* xb,
-                              const Acc& acc) {
+// The same pass in FP32 with every product on packed pairs (two FP32 FMAs
+// per instruction), as in tricubic_pair: rows y and y+1 of a slice come as one
+// float2 per x tap from `rows` (PairRows: the row-pair array; SingleRows: the
+// single layout, two loads per tap pair). base: the single-layout index of
+// voxel (cx-1, cy-1, cz-1), where the tap cotangents go.
+template <typename Acc, typename Rows>
+SRT_HD void tricubic_vjp_pair(const Rows& rows, int64_t base, int64_t px, int64_t pxy, float tx, float ty, float tz,
+                              const float* qb, Tri<float>& Q, float* xb, const Acc& acc) {
   CRW4<float> X, Y, Z;
   cr_weights4(tx, X);
   cr_weights4(ty, Y);
@@ -254,7 +266,7 @@ SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64
   // taps of the next slice, loaded while the current one is processed
   float2 nt[8];
   for (int pr = 0; pr < 2; ++pr)
-    for (int i = 0; i < 4; ++i) nt[4 * pr + i] = ldg(f + basep + 2 * pr * px + i);
+    for (int i = 0; i < 4; ++i) nt[4 * pr + i] = rows(0, pr, i);
 #pragma unroll 1
   for (int c = 0; c < 4; ++c) {
     float2 s00 = z0, s01 = z0, s02 = z0, s03 = z0, s10 = z0, s11 = z0, s12 = z0, s20 = z0, s21 = z0, s30 = z0;
@@ -269,7 +281,7 @@ SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64
     for (int i = 0; i < 8; ++i) ct[i] = nt[i];
     if (c < 3)
       for (int pr = 0; pr < 2; ++pr)
-        for (int i = 0; i < 4; ++i) nt[4 * pr + i] = ldg(f + basep + (c + 1) * pxy2 + 2 * pr * px + i);
+        for (int i = 0; i < 4; ++i) nt[4 * pr + i] = rows(c + 1, pr, i);
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
       const float2 t0 = ct[4 * pr], t1 = ct[4 * pr + 1], t2 = ct[4 * pr + 2], t3 = ct[4 * pr + 3];
@@ -339,15 +351,19 @@ SRT_HD void tricubic_vjp_pair(const float2* __restrict__ f, int64_t basep, int64
            qb[6] * o102 + qb[7] * o021 + qb[8] * o012 + qb[9] * o003;
 }
 
-// One field's pass: the packed form on the row-pair array (PAIR, FP32 only)
-// or the plain one.
+// One field's pass: FP32 (MIXED) in the packed form, reading the row-pair
+// array (PAIR) or the single layout; FP64 in the plain form.
 template <bool PAIR, typename T, typename Acc>
 SRT_HD void field_pass(const float* f, const float2* fp, int64_t base, int64_t basep, const Geom& G, const T* t,
                        const T* qb, Tri<T>& Q, T* xb, const Acc& acc) {
-  if constexpr (PAIR)
-    tricubic_vjp_pair<Acc>(fp, basep, base, G.px, G.pxy, G.pxy2, t[0], t[1], t[2], qb, Q, xb, acc);
-  else
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if constexpr (PAIR)
+      tricubic_vjp_pair<Acc>(PairRows{fp, basep, G.px, G.pxy2}, base, G.px, G.pxy, t[0], t[1], t[2], qb, Q, xb, acc);
+    else
+      tricubic_vjp_pair<Acc>(SingleRows{f, base, G.px, G.pxy}, base, G.px, G.pxy, t[0], t[1], t[2], qb, Q, xb, acc);
+  } else {
     tricubic_vjp<T, Acc>(f, base, G.px, G.pxy, t[0], t[1], t[2], qb, Q, xb, acc);
+  }
 }
 
 // -------------------------------------------------------- stage and core

@@ -312,6 +312,7 @@ int srt_fields_destroy(srt_fields* f) {
 }
 
 int srt_release_cached_memory(void) {
+  noalloc_forget_scratch();
   int n = 0;
   cudaGetDeviceCount(&n);
   int prev = 0;

@@ -76,6 +76,9 @@ cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* 
 // FP64 re-trace of the rays listed by a MIXED trace (count read on the device).
 cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels);
 
+// Forgets srt_forward_noalloc's cached scratch addresses (srt_noalloc.cu).
+void noalloc_forget_scratch();
+
 // Peak issue-rate probes (FMA loop kernels); returns achieved FLOP/s.
 cudaError_t probe_fma(int kind, double* flops_per_s);
 

@@ -27,7 +27,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <mutex>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -696,6 +698,10 @@ struct Reader {
           stack.push_back(child);
           continue;
         }
+        // a chunk's stored size cannot exceed the file (a corrupt size would
+        // otherwise make a worker allocate up to 4 GiB before its read fails)
+        if (child == kUndef || base + child > F.size || csz > F.size - (base + child))
+          fail(SRT_ERR_FORMAT, "chunk extends past the end of the file");
         leaves.push_back(Leaf{child, csz, mask, origin});
       }
     }
@@ -718,6 +724,17 @@ struct Reader {
         } catch (const H5Error& e) {
           std::lock_guard<std::mutex> lock(err_mutex);
           if (!failed) first = e;
+          failed = true;
+          next = leaves.size();
+        } catch (const std::bad_alloc&) {
+          // an exception that left a worker thread would end the process
+          std::lock_guard<std::mutex> lock(err_mutex);
+          if (!failed) first = H5Error{SRT_ERR_OUT_OF_MEMORY, "out of host memory while reading chunks"};
+          failed = true;
+          next = leaves.size();
+        } catch (const std::exception& e) {
+          std::lock_guard<std::mutex> lock(err_mutex);
+          if (!failed) first = H5Error{SRT_ERR_FORMAT, std::string("chunk read failed: ") + e.what()};
           failed = true;
           next = leaves.size();
         }

@@ -138,8 +138,11 @@ __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ?
 // double-float arithmetic on the FP32 pipes (srt_dd.cuh; trajectory ~1e-14
 // from the FP64 one, maps within one float ulp), which is shorter once the
 // warps outnumber the SM sub-partitions.
-constexpr int64_t kRefineMaxBlocks = 152 * 32;
-constexpr int64_t kRefineGroupMaxRays = 2 * 608 * 8;
+// Re-trace grid: at most 32 one-warp blocks per SM (the SM count is read from
+// the device); lists up to two warps per SM sub-partition (8 rays per warp)
+// take the FP64 path.
+constexpr int64_t kRefineBlocksPerSM = 32;
+constexpr int64_t kRefineWarpsPerSubpartition = 2;
 
 __device__ __forceinline__ void shfl_tri(Tri<double>& d, const Tri<double>& s, int src, unsigned mask) {
   d.v = __shfl_sync(mask, s.v, src);
@@ -285,9 +288,13 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t d
 }
 
 cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels) {
-  int64_t dd_min = kRefineGroupMaxRays;
-  if (const char* e = getenv("SRT_REFINE_DD_MIN")) dd_min = strtoll(e, nullptr, 10);
-  const int64_t blocks = std::min((a.pix_count + 7) / 8, kRefineMaxBlocks);
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  int64_t dd_min = kRefineWarpsPerSubpartition * 4 * (int64_t)sms * 8;
+  if (const char* v = getenv("SRT_REFINE_DD_MIN")) dd_min = strtoll(v, nullptr, 10);
+  const int64_t blocks = std::min((a.pix_count + 7) / 8, kRefineBlocksPerSM * (int64_t)sms);
   if (blocks < 1) return cudaSuccess;
   refine_kernel<4><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min);
   refine_kernel<1><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min);

@@ -18,7 +18,13 @@
 //     (cudaGetSymbolAddress, with that device current) and caches it; make
 //     that first call before any stream capture;
 //   * every call shares the array: the counter is cleared on the stream at the
-//     start of each call, and calls whose work overlaps on the GPU race for it.
+//     start of each call, and calls whose work overlaps on the GPU race for it;
+//   * the cached address belongs to the device's primary context: after
+//     cudaDeviceReset (or anything else that tears that context down) call
+//     srt_release_cached_memory, which forgets it, before the next call;
+//   * flags: SRT_ASYNC, SRT_NESTED_RANGE and SRT_MIXED_NO_REFINE act as in
+//     srt_forward (SRT_OUTPUT_DEVICE is implied and accepted); any other flag
+//     is refused with SRT_ERR_UNSUPPORTED rather than ignored.
 #include <mutex>
 #include "srt_internal.h"
 
@@ -60,6 +66,15 @@ int scratch_for(int dev, DeviceScratch* out) {
 
 }  // namespace
 
+namespace srt {
+// Forgets the cached scratch addresses (srt_release_cached_memory calls this,
+// so that a context torn down and made again gets its addresses looked up anew).
+void noalloc_forget_scratch() {
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  for (int d = 0; d < kMaxDevices; ++d) g_scratch[d] = DeviceScratch();
+}
+}  // namespace srt
+
 extern "C" int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int64_t pix_begin, int64_t pix_count,
                                    int n_steps, int precision, float* const maps[SRT_NUM_MAPS], unsigned flags,
                                    void* stream) {
@@ -75,6 +90,14 @@ extern "C" int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int6
                      "srt_forward_noalloc: %lld rays requested, at most %lld per call (trace larger ranges in parts "
                      "or with srt_forward)",
                      (long long)pix_count, (long long)kNoAllocMaxRays);
+  const unsigned known = SRT_ASYNC | SRT_NESTED_RANGE | SRT_MIXED_NO_REFINE | SRT_OUTPUT_DEVICE;
+  if (flags & ~known)
+    return set_error(SRT_ERR_UNSUPPORTED, "srt_forward_noalloc: flags 0x%x not supported (SRT_ASYNC, SRT_NESTED_RANGE, "
+                     "SRT_MIXED_NO_REFINE; maps are always device buffers)", flags & ~known);
+  const bool nested = (flags & SRT_NESTED_RANGE) != 0;
+  if (nested && (nside & (nside - 1)) != 0)
+    return set_error(SRT_ERR_INVALID_ARGUMENT,
+                     "srt_forward_noalloc: NESTED pixel ranges need a power-of-two nside, got %lld", (long long)nside);
   if (n_steps < 1 || n_steps > (1 << 22))
     return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_forward_noalloc: invalid n_steps %d", n_steps);
   if (precision != SRT_PRECISION_MIXED && precision != SRT_PRECISION_FP64)
@@ -103,12 +126,13 @@ extern "C" int srt_forward_noalloc(const srt_fields* fields, int64_t nside, int6
     int l = 0;
     while ((int64_t(1) << l) < nside) ++l;
     a.log2p = l;
-    a.launch_rays = 12 * (int64_t(1) << (2 * l));
+    a.launch_rays = nested ? pix_count : 12 * (int64_t(1) << (2 * l));
     a.pix_begin = pix_begin;
     a.pix_count = pix_count;
+    a.nested = nested;
     a.n_steps = n_steps;
     for (int m = 0; m < 6; ++m) a.maps[m] = maps[m];
-    const bool refine = precision == SRT_PRECISION_MIXED;
+    const bool refine = precision == SRT_PRECISION_MIXED && !(flags & SRT_MIXED_NO_REFINE);
     a.refine_list = refine ? sc.list : nullptr;
     a.refine_count = refine ? sc.count : nullptr;
     cudaError_t e = cudaSuccess;

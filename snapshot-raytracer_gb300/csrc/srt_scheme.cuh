@@ -197,14 +197,36 @@ SRT_HD float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.
 #endif
 SRT_HD float2 dup2(float v) { return make_float2(v, v); }
 
-// The same interpolation as `tricubic`, from the row-pair array: rows y and
-// y+1 of a slice arrive together in one 64-bit load per x tap, and every
-// pass runs on packed pairs (two FP32 FMAs per instruction): the x pass on
-// the two rows at once with duplicated x weights, the y pass with the weights
-// of rows (0, 1) and (2, 3), the z pass on even/odd partial sums that are
-// added at the end. base: the pair index of voxel (cx-1, cy-1, cz-1).
-SRT_HD void tricubic_pair(const float2* __restrict__ f, int64_t base, int64_t px, int64_t pxy2, const CRW<float>& X,
-                          const CRW<float>& Y, const CRW<float>& Z, Tri<float>& r) {
+// Where the packed passes get their taps: rows y and y+1 of a slice, tap i,
+// as one float2. Two sources:
+//   PairRows   the row-pair array (srt_fields.pr): one 64-bit load per tap
+//              pair; base is the pair index of voxel (cx-1, cy-1, cz-1);
+//   SingleRows the halo-padded single layout: two 32-bit loads (rows y and
+//              y+1, one row stride apart) placed in the two halves of the
+//              pair, so the packed arithmetic needs no second copy of the
+//              field; base is the voxel's padded index.
+// Both give the same float2 values, so the interpolations agree bit for bit.
+struct PairRows {
+  const float2* __restrict__ f;
+  int64_t base, px, pxy2;
+  SRT_HD float2 operator()(int c, int pr, int i) const { return ldg(f + base + c * pxy2 + 2 * pr * px + i); }
+};
+struct SingleRows {
+  const float* __restrict__ f;
+  int64_t base, px, pxy;
+  SRT_HD float2 operator()(int c, int pr, int i) const {
+    const float* r = f + base + c * pxy + 2 * pr * px + i;
+    return make_float2(ldg(r), ldg(r + px));
+  }
+};
+
+// The same interpolation as `tricubic` with every pass on packed pairs (two
+// FP32 FMAs per instruction): the x pass on rows y and y+1 at once with
+// duplicated x weights, the y pass with the weights of rows (0, 1) and
+// (2, 3), the z pass on even/odd partial sums that are added at the end.
+template <typename Rows>
+SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float>& Y, const CRW<float>& Z,
+                          Tri<float>& r) {
   float2 xw[4], xg[4], xh[4];
   for (int i = 0; i < 4; ++i) {
     xw[i] = dup2(X.w[i]);
@@ -221,8 +243,7 @@ SRT_HD void tricubic_pair(const float2* __restrict__ f, int64_t base, int64_t px
     float2 A = z0, AY = z0, AYY = z0, AX = z0, AXY = z0, AXX = z0;
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
-      const float2* row = f + base + c * pxy2 + 2 * pr * px;
-      const float2 t0 = ldg(row + 0), t1 = ldg(row + 1), t2 = ldg(row + 2), t3 = ldg(row + 3);
+      const float2 t0 = rows(c, pr, 0), t1 = rows(c, pr, 1), t2 = rows(c, pr, 2), t3 = rows(c, pr, 3);
       float2 RV = fmul2(xw[0], t0), RX = fmul2(xg[0], t0), RXX = fmul2(xh[0], t0);
       RV = ffma2(xw[1], t1, RV);
       RX = ffma2(xg[1], t1, RX);
@@ -765,11 +786,11 @@ SRT_HD void add_b_component(const FieldPtrs& F, const Geom& G, const int* cc, co
   const int cx = C == 0 ? cs[0] : cc[0], cy = C == 1 ? cs[1] : cc[1], cz = C == 2 ? cs[2] : cc[2];
   Tri<float> r;
   if (PAIR)
-    tricubic_pair(F.pr[C], cell_base_pair(G, cx, cy, cz), G.px, G.pxy2, C == 0 ? S : Cx, C == 1 ? S : Cy,
+    tricubic_pair(PairRows{F.pr[C], cell_base_pair(G, cx, cy, cz), G.px, G.pxy2}, C == 0 ? S : Cx, C == 1 ? S : Cy,
                   C == 2 ? S : Cz, r);
   else
-    tricubic<float, float>(F.b[C], cell_base(G, cx, cy, cz), G.px, G.pxy, C == 0 ? S : Cx, C == 1 ? S : Cy,
-                           C == 2 ? S : Cz, r);
+    tricubic_pair(SingleRows{F.b[C], cell_base(G, cx, cy, cz), G.px, G.pxy}, C == 0 ? S : Cx, C == 1 ? S : Cy,
+                  C == 2 ? S : Cz, r);
   A.val[C] = r.v;
   for (int i = 0; i < 3; ++i) A.ngB[i] += r.g[i] * n[C];
   const float gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
@@ -873,9 +894,9 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   add_b_component<2, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
   Tri<float> p;
   if (PAIR)
-    tricubic_pair(F.pr[3], cell_base_pair(G, cc[0], cc[1], cc[2]), G.px, G.pxy2, Cx, Cy, Cz, p);
+    tricubic_pair(PairRows{F.pr[3], cell_base_pair(G, cc[0], cc[1], cc[2]), G.px, G.pxy2}, Cx, Cy, Cz, p);
   else
-    tricubic<float, float>(F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy, Cx, Cy, Cz, p);
+    tricubic_pair(SingleRows{F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy}, Cx, Cy, Cz, p);
 
   const float dA = s + d[12];
   const float dAp = d[13] - 1.f;

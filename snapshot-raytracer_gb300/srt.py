@@ -30,7 +30,7 @@ SRT_MIXED_NO_REFINE = 64
 SRT_NESTED_RANGE = 128
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
-          -5: "format error", -6: "no CUDA device", -7: "unsupported"}
+          -5: "format error", -6: "no CUDA device", -7: "unsupported", -8: "overflow"}
 
 
 class SrtError(RuntimeError):

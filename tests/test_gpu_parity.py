@@ -272,3 +272,26 @@ def test_constant_gradient_potential_analytic(srt, orc, precision):
     with srt.Fields(phi, b) as f:
         maps, _ = f.forward(nside, S, precision=precision)
     check_linear_phi_maps(maps, nside, S, predict, orc.pix2ang_ring)
+
+
+def test_single_layout_packed_path_equals_pair_layout(srt):
+    """The MIXED forward and vjp read their packed tap pairs either from the
+    row-pair copy of the fields or, with SRT_FIELDS_NO_PAIRS, from the single
+    halo layout (two loads per pair): the float2 values and every operation
+    are the same, so the maps, the refined-ray counts and the deterministic
+    gradients agree bit for bit."""
+    import srt_fields
+
+    phi, b = srt_fields.gaussian_fields_np(48, seed=17)
+    nside, steps = 16, 48
+    w = np.random.default_rng(5).standard_normal((6, 12 * nside * nside)).astype(np.float32)
+    out = {}
+    for pairs in (True, False):
+        with srt.Fields(phi, b, pairs=pairs) as f:
+            m, st = f.forward(nside, steps, precision="mixed")
+            g, gb, _ = f.vjp(nside, steps, w, precision="mixed", deterministic=True, ckpt_every=7)
+            out[pairs] = (m, st.refined_rays, g, gb)
+    assert np.array_equal(out[True][0].view(np.uint32), out[False][0].view(np.uint32))
+    assert out[True][1] == out[False][1]
+    assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
+    assert np.array_equal(out[True][3].view(np.uint32), out[False][3].view(np.uint32))

@@ -168,3 +168,24 @@ def test_forward_tape_vjp_pair(srt):
         ga, ba, _ = tape.vjp(wpart)  # FP32 atomics
         assert np.abs(ga - g1).max() <= 1e-4 * np.abs(g1).max()
         tape.close()
+
+
+def test_vjp_deterministic_range_overflow_is_an_error(srt):
+    """The deterministic mode's 64-bit fixed point holds |gradient| < 2^30 per
+    voxel; weights that drive the gradient past it make srt_vjp fail with
+    SRT_ERR_OVERFLOW (-8) instead of returning wrapped sums, while the FP32
+    accumulation of the same call stays finite, and a call within range after
+    it succeeds."""
+    phi, b, nside, steps, w = _case(n=16, nside=2, steps=10, seed=3)
+    big = (w * np.float32(1e20)).astype(np.float32)
+    with srt.Fields(phi, b) as f:
+        with pytest.raises(srt.SrtError) as ei:
+            f.vjp(nside, steps, big, precision="mixed", deterministic=True)
+        assert ei.value.code == -8 and "fixed-point range" in str(ei.value)
+        with pytest.raises(srt.SrtError) as ei:
+            f.vjp(nside, steps, big, precision="fp64", deterministic=True)
+        assert ei.value.code == -8
+        g, gb, _ = f.vjp(nside, steps, big, precision="mixed")
+        assert np.all(np.isfinite(g)) and np.abs(g).max() > 2.0 ** 31
+        g1, _, _ = f.vjp(nside, steps, w, precision="mixed", deterministic=True)
+        assert np.all(np.isfinite(g1)) and np.abs(g1).max() < 2.0 ** 30

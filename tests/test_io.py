@@ -178,6 +178,28 @@ def test_h5_reader_many_chunks_in_parallel_and_a_corrupt_chunk(srt, tmp_path):
     assert "corrupt deflate chunk" in str(ei.value)
 
 
+def test_h5_reader_chunk_size_past_end_of_file(srt, tmp_path):
+    """A chunk whose stored size (a 32-bit field of its B-tree entry) is
+    corrupt and reaches past the end of the file is refused with a format
+    error before anything is allocated for it, whichever thread reads it."""
+    import struct
+
+    import h5_variants
+
+    a = np.random.default_rng(7).standard_normal((20, 18, 22)).astype(np.float32)
+    p = str(tmp_path / "ok.h5")
+    h5_variants.write_v2_chunked(p, a, chunk=(5, 6, 4))
+    raw = bytearray(open(p, "rb").read())
+    at = raw.index(b"TREE" + bytes([1, 0]))  # first leaf node
+    entry = at + 8 + 16                      # after signature, type, level, count and two sibling addresses
+    raw[entry:entry + 4] = struct.pack("<I", 0xFFFFFF00)
+    q = str(tmp_path / "huge_chunk.h5")
+    open(q, "wb").write(bytes(raw))
+    with pytest.raises(srt.SrtError) as ei:
+        srt.h5_read_scalar(q)
+    assert ei.value.code == -5 and "past the end" in str(ei.value)
+
+
 @pytest.mark.parametrize("fanout", [64, 3])
 def test_h5_reader_multilevel_chunk_btree(srt, tmp_path, fanout):
     """Chunk B-trees of several levels, as libhdf5 writes them for many chunks

@@ -110,3 +110,33 @@ def test_field_cotangents_against_linearity(adj):
             assert abs(got - want) <= 1e-9 * (abs(want) + 1e-12), (c, got, want)
         # taps outside the ray's 4x4x4 footprints get nothing
         assert sum(int(np.count_nonzero(gc)) for gc in g) <= 4 * 64
+
+
+def test_mixed_sweep_indices_stay_in_the_padded_grids(adj):
+    """Index audit of the MIXED sweep's field passes, built for the host: every
+    tap read and every tap-cotangent row of rhs_vjp on stage_view_mixed (the
+    arithmetic of sweep_kernel_mixed) for rays in all directions at affine
+    distances up to several box lengths (positions wrap around the periodic
+    box), with perturbations up to a few cells, stays inside the halo-padded
+    grid, and the row-pair reads inside the row-pair array. The fields are
+    zero: only the indices are checked."""
+    import ctypes
+
+    adj.audit_vjp_indices_mixed.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p] * 5
+    rng = np.random.default_rng(12)
+    for n0, n1, n2 in ((12, 12, 12), (16, 20, 24), (7, 5, 9)):
+        count = 4000
+        theta = np.arccos(rng.uniform(-1, 1, count))
+        phi = rng.uniform(0, 2 * np.pi, count)
+        s = np.concatenate([rng.uniform(0, 4 * max(n0, n1, n2), count - 8),
+                            np.array([0, 0.5, 1, n0 / 2, n0 / 2 + 0.5, n0, 2 * n0, 3.5 * n0])]).astype(np.float32)
+        d = (rng.standard_normal((count, 19)) * rng.choice([1e-6, 1e-3, 2.0], (count, 1))).astype(np.float32)
+        # positions exactly on faces of both grids
+        d[:16, :3] = 0
+        out = np.zeros(5, np.int64)
+        adj.audit_vjp_indices_mixed(n0, n1, n2, count, theta.ctypes.data, phi.ctypes.data, s.ctypes.data,
+                                    d.ctypes.data, out.ctypes.data)
+        lo, hi, hip, pvox, npair = (int(x) for x in out)
+        assert lo >= 0, (n0, n1, n2, lo)
+        assert hi < pvox, (n0, n1, n2, hi, pvox)
+        assert hip < npair, (n0, n1, n2, hip, npair)
