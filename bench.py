@@ -79,6 +79,9 @@ def parse():
     ap.add_argument("--n-steps", type=int, default=512)
     ap.add_argument("--precision", default="mixed", choices=("mixed", "fp64", "ref16"))
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-pairs", dest="pairs", action="store_false",
+                    help="lay the fields out without their row-pair copies (SRT_FIELDS_NO_PAIRS): the packed MIXED "
+                         "passes then form their tap pairs from the single layout")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--compare-batch", type=int, default=5, help="batch used for the FP64 / REF16 legs (-1: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
@@ -430,12 +433,13 @@ def run_ours(args):
            "grid": n, "nside": nside, "rays": npix, "n_steps": S, "precision": args.precision,
            "fields": "gaussian P(k)~k^-3, phi rms 1e-5, B rms 1e-7, seed %d" % (args.seed + rank),
            "l2": "inputs larger than L2 (%.1f GB of fields vs 0.13 GB L2)" % (16 * n ** 3 / 1e9),
-           "parallelism": "replicas x%d (pixel-parallel, no collective)" % world}
+           "parallelism": "replicas x%d (pixel-parallel, no collective)" % world,
+           "field_layout": "halo-padded planes" + (" + row-pair copies" if args.pairs else "")}
 
     phi_d, b_d = srt_fields.gaussian_fields_torch(n, seed=args.seed + rank, device=dev)
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
-    fields = srt.Fields(phi_d, b_d, stream=stream)
+    fields = srt.Fields(phi_d, b_d, stream=stream, pairs=args.pairs)
     if args.e2e_steps <= 0:  # the laid-out copy is all the trace needs (2048^3: 137 GB freed)
         torch.cuda.synchronize()
         del phi_d, b_d
@@ -514,7 +518,7 @@ def run_ours(args):
             barrier(world)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            f = srt.Fields(phi_np, b_np)
+            f = srt.Fields(phi_np, b_np, pairs=args.pairs)
             ta = time.perf_counter()
             f.forward(nside, S, precision=args.precision, out=maps_h)
             tb = time.perf_counter()
@@ -531,7 +535,7 @@ def run_ours(args):
                          "split_ms": {"fields_create_upload": float(sp[0]), "forward_and_maps_back": float(sp[1]),
                                       "fields_release": float(sp[2])},
                          "create_ms_each": [round(x[0], 1) for x in split]}
-        fields = srt.Fields(phi_np, b_np)
+        fields = srt.Fields(phi_np, b_np, pairs=args.pairs)
     else:
         phi_np = b_np = None
 
@@ -582,9 +586,11 @@ def run_ours(args):
         from oracle import oracle
 
         cores = oracle.max_threads()
-        rays, dt = time_cpu(lambda pix: oracle.trace_pixels(phi_np, b_np, nside, S, pix, mode="fp64",
-                                                            threads=cores),
-                            args.cpu_seconds, lambda k: sample_pixels(nside, k, seed=2))
+        # the fields are laid out once, outside the timed calls, as the GPU
+        # arm's fields are resident before its timed region
+        with oracle.Fields(phi_np, b_np, mode="fp64") as of:
+            rays, dt = time_cpu(lambda pix: of.trace_pixels(nside, S, pix, threads=cores),
+                                args.cpu_seconds, lambda k: sample_pixels(nside, k, seed=2))
         result["cpu_baseline"] = {"value": rays * S / dt, "unit": "ray-steps/s", "cores": cores, "kind": "port",
                                   "sample": "%d random pixels of the same workload x %d steps, FP64 oracle, "
                                             "%.1f s" % (rays, S, dt)}

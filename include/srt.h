@@ -66,7 +66,8 @@ extern "C" {
 /* flags */
 #define SRT_INPUT_DEVICE 1u  /* srt_fields_create: phi / b point to device memory */
 #define SRT_OUTPUT_DEVICE 2u /* srt_forward / srt_vjp: outputs are device memory */
-#define SRT_ASYNC 4u         /* do not synchronise; order work on `stream` */
+#define SRT_ASYNC 4u         /* do not synchronise; order work on `stream` (host
+                                buffers must stay valid until it completes) */
 #define SRT_ACCUMULATE 8u    /* srt_vjp: add into the gradient grids instead of
                                 overwriting them */
 #define SRT_DETERMINISTIC 16u /* srt_vjp: order-independent (bitwise
@@ -74,6 +75,9 @@ extern "C" {
 #define SRT_FIELDS_NO_PAIRS 32u /* srt_fields_create: do not build the row-pair
                                    copies of the fields (2x the field memory)
                                    that the MIXED forward reads when present */
+#define SRT_FIELDS_STAGED 256u /* srt_fields_create: copy host inputs through a
+                                  device slab even when they are mapped pinned
+                                  memory the layout kernel could read directly */
 #define SRT_MIXED_NO_REFINE 64u /* srt_forward, MIXED: keep the FP32 result of
                                    rays that passed within 1e-7 cell of a cell
                                    face instead of re-tracing them in FP64 */
@@ -118,8 +122,11 @@ int srt_device_count(void);
  * before and two after on every axis, one FP32 plane per B component.
  * phi: n0*n1*n2 floats; b_xyz: 3*n0*n1*n2 floats interleaved per voxel
  * (B_x, B_y, B_z of voxel v at b_xyz[3v+0..2]), the layout of the reference's
- * HDF5 vector read (snapshot-raytracer.cu:89-186). Host inputs are streamed
- * in slabs, so peak device memory is the laid-out fields plus one slab.
+ * HDF5 vector read (snapshot-raytracer.cu:89-186). Host inputs in mapped
+ * pinned memory (cudaHostAlloc, or cudaHostRegister with mapping) are read by
+ * the layout kernel directly over the host link; other host inputs (or all,
+ * with SRT_FIELDS_STAGED) are streamed through a device slab, so peak device
+ * memory is the laid-out fields plus one slab.
  * Unless SRT_FIELDS_NO_PAIRS, and when device memory allows, each field is
  * also stored as row pairs (f(i,j,k), f(i,j+1,k)) for the packed-FMA MIXED
  * forward; without them MIXED reads the single copy.

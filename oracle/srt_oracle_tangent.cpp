@@ -150,9 +150,14 @@ extern "C" int srto_tangent(const float* phi, const float* b_xyz, int64_t n0, in
   if (ndir < 0 || ndir > K || n0 < 1 || n1 < 1 || n2 < 1 || n_steps < 1 || count < 0) return -1;
   const int64_t nv = n0 * n1 * n2;
   std::vector<float> planes((size_t)(3 * nv));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : omp_get_max_threads())
+#endif
   for (int64_t v = 0; v < nv; ++v)
     for (int c = 0; c < 3; ++c) planes[c * nv + v] = b_xyz[3 * v + c];
-  std::vector<float> dplanes((size_t)(3 * nv * (ndir > 0 ? ndir : 1)));
+  bool any_db = false;
+  for (int k = 0; k < ndir; ++k) any_db = any_db || (dir_b && dir_b[k]);
+  std::vector<float> dplanes(any_db ? (size_t)(3 * nv * ndir) : 0);
   tan_fields F;
   std::memset(&F, 0, sizeof(F));
   F.n[0] = n0;

@@ -215,10 +215,10 @@ __global__ void __launch_bounds__(128, 2) segment_kernel_mixed(const AdjArgs A, 
 // while the current stage runs); l carried in lam between segments. l and the
 // running sum of the a's live in shared memory (one column per thread) to keep
 // registers for the field passes.
-template <typename Acc, bool PAIR>
+template <typename AccB, typename AccP, bool PAIR>
 __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t slot, const MixedRay& R,
-                                              const float* x0, float* lam, const Acc* acc, float (*s_lam)[128],
-                                              float (*s_tot)[128]) {
+                                              const float* x0, float* lam, const AccB* accb, const AccP& accp,
+                                              float (*s_lam)[128], float (*s_tot)[128]) {
   const int t = threadIdx.x;
   for (int j = 0; j < 19; ++j) s_lam[j][t] = lam[(int64_t)j * A.count + slot];
   const float* tape = (const float*)A.seg + slot;
@@ -247,7 +247,7 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
       for (int j = 0; j < 19; ++j) u[j] = ld_stream(tape + ((int64_t)(qn >> 2) * kTapeStep + 19 * (qn & 3) + j) * A.count);
     }
     for (int j = 0; j < 19; ++j) an[j] = 0.f;
-    rhs_vjp<float, Acc, PAIR>(V, A.F, A.G, fb, an, acc);
+    rhs_vjp<float, AccB, AccP, PAIR>(V, A.F, A.G, fb, an, accb, accp);
     for (int j = 0; j < 19; ++j) s_tot[j][t] += an[j];
     if (stage == 0)
       for (int j = 0; j < 19; ++j) s_lam[j][t] += s_tot[j][t];
@@ -255,14 +255,22 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
   for (int j = 0; j < 19; ++j) lam[(int64_t)j * A.count + slot] = s_lam[j][t];
 }
 
-template <typename Acc, bool PAIR>
+// BGRAD: the B gradient is wanted (else the B passes are compiled without a
+// scatter).
+template <typename Acc, bool PAIR, bool BGRAD>
 __global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, int sgi, float* lam, const Acc a0,
                                                            const Acc a1, const Acc a2, const Acc a3) {
   __shared__ float s_lam[19][128];
   __shared__ float s_tot[19][128];
   const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= A.count) return;
-  const Acc acc[4] = {a0, a1, a2, a3};
+  typedef typename std::conditional<BGRAD, Acc, AccNone>::type AccB;
+  AccB accb[3];
+  if constexpr (BGRAD) {
+    accb[0] = a0;
+    accb[1] = a1;
+    accb[2] = a2;
+  }
   const RayDir d = ray_dir_pix(A.nside, A.rays[slot]);
   MixedRay R;
   float x0[3];
@@ -271,7 +279,20 @@ __global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, in
     init_mixed(d, R, y);
   }
   mixed_observer(A.G, x0);
-  sweep_segment<Acc, PAIR>(A, sgi, slot, R, x0, lam, acc, s_lam, s_tot);
+  sweep_segment<AccB, Acc, PAIR>(A, sgi, slot, R, x0, lam, accb, a3, s_lam, s_tot);
+}
+
+template <typename Acc>
+void launch_sweep(const AdjArgs& A, int sgi, float* lam, const Acc* a, bool pair, bool bgrad, unsigned blocks,
+                  cudaStream_t s) {
+  if (pair && bgrad)
+    sweep_kernel_mixed<Acc, true, true><<<blocks, 128, 0, s>>>(A, sgi, lam, a[0], a[1], a[2], a[3]);
+  else if (pair)
+    sweep_kernel_mixed<Acc, true, false><<<blocks, 128, 0, s>>>(A, sgi, lam, a[0], a[1], a[2], a[3]);
+  else if (bgrad)
+    sweep_kernel_mixed<Acc, false, true><<<blocks, 128, 0, s>>>(A, sgi, lam, a[0], a[1], a[2], a[3]);
+  else
+    sweep_kernel_mixed<Acc, false, false><<<blocks, 128, 0, s>>>(A, sgi, lam, a[0], a[1], a[2], a[3]);
 }
 
 // ------------------------------------------------------------- FP64 mode
@@ -361,7 +382,7 @@ __global__ void __launch_bounds__(128) reverse_kernel_fp64(const AdjArgs A, cons
         stage_view_fp64(u, A.G, V);
         double ub[19];
         for (int j = 0; j < 19; ++j) ub[j] = 0.0;
-        rhs_vjp<double, Acc>(V, A.F, A.G, fb, ub, acc);
+        rhs_vjp<double, Acc, Acc>(V, A.F, A.G, fb, ub, acc, acc[3]);
         for (int j = 0; j < 19; ++j) {
           anext[j] = ub[j];
           atot[j] += ub[j];
@@ -695,20 +716,16 @@ static int vjp_impl(const srt_fields* fields, int64_t nside, int64_t pix_begin, 
         make_acc<AccF32, float4>(af, A.acc);
         make_acc<AccFixed, unsigned long long>(ax, A.acc);
         for (int fld = 0; fld < 4; ++fld) ax[fld].ovf = (unsigned*)ovf.p;
+        const bool bgrad = db_xyz != nullptr;
         for (int sgi = nseg - 1; sgi >= 0; --sgi) {
           if (pair)
             segment_kernel_mixed<true><<<blocks, 128, 0, s>>>(A, sgi);
           else
             segment_kernel_mixed<false><<<blocks, 128, 0, s>>>(A, sgi);
-          if (determ && pair)
-            sweep_kernel_mixed<AccFixed, true><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, ax[0], ax[1], ax[2], ax[3]);
-          else if (determ)
-            sweep_kernel_mixed<AccFixed, false><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, ax[0], ax[1], ax[2],
-                                                                      ax[3]);
-          else if (pair)
-            sweep_kernel_mixed<AccF32, true><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, af[0], af[1], af[2], af[3]);
+          if (determ)
+            launch_sweep<AccFixed>(A, sgi, (float*)lam.p, ax, pair, bgrad, blocks, s);
           else
-            sweep_kernel_mixed<AccF32, false><<<blocks, 128, 0, s>>>(A, sgi, (float*)lam.p, af[0], af[1], af[2], af[3]);
+            launch_sweep<AccF32>(A, sgi, (float*)lam.p, af, pair, bgrad, blocks, s);
           kernels += 2;
         }
       }

@@ -134,6 +134,15 @@ struct AccFixed {
   }
 };
 
+// No accumulation: the B components' passes when only the phi gradient is
+// wanted. active() is false at compile time, so those passes are compiled
+// without their scatter (less code, fewer registers).
+struct AccNone {
+  SRT_HD constexpr bool active() const { return false; }
+  template <typename V>
+  SRT_HD void add_row(int64_t, V, V, V, V) const {}
+};
+
 // ------------------------------------------------- fused field pass (vjp)
 
 // Interpolates one field (value, gradient, Hessian into Q; third derivatives
@@ -449,10 +458,11 @@ SRT_HD void vjp_b_component(const StageView<T>& V, const FieldPtrs& F, const Geo
   bb[C] += T(0.5) * e2b * gn;
 }
 
-// yb += J(u)^T fb for the stage described by V; tap cotangents go to acc[0..3]
-// (B_x, B_y, B_z, phi).
-template <typename T, typename Acc, bool PAIR = false>
-SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, const T* fb, T* yb, const Acc* acc) {
+// yb += J(u)^T fb for the stage described by V; tap cotangents go to accb[0..2]
+// (B_x, B_y, B_z) and accp (phi).
+template <typename T, typename AccB, typename AccP, bool PAIR = false>
+SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, const T* fb, T* yb, const AccB* accb,
+                    const AccP& accp) {
   const T* n = V.n;
   const T* a = V.a;
   const T* b = V.b;
@@ -511,12 +521,12 @@ SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, co
   T ngB[3] = {0, 0, 0}, e1ngB = 0, e2ngB = 0, nlap = 0, Tm[6] = {0, 0, 0, 0, 0, 0};
 
   // ---- B components (compile-time component index: no local-memory arrays)
-  vjp_b_component<0, PAIR, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[0], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
-                             Tm);
-  vjp_b_component<1, PAIR, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[1], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
-                             Tm);
-  vjp_b_component<2, PAIR, T, Acc>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, acc[2], xb, nb, ab, bb, ngB, e1ngB, e2ngB, nlap,
-                             Tm);
+  vjp_b_component<0, PAIR, T, AccB>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, accb[0], xb, nb, ab, bb, ngB, e1ngB, e2ngB,
+                                    nlap, Tm);
+  vjp_b_component<1, PAIR, T, AccB>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, accb[1], xb, nb, ab, bb, ngB, e1ngB, e2ngB,
+                                    nlap, Tm);
+  vjp_b_component<2, PAIR, T, AccB>(V, F, G, fb, ngBb, e1b, e2b, nlapb, Tb, accb[2], xb, nb, ab, bb, ngB, e1ngB, e2ngB,
+                                    nlap, Tm);
 
   // ---- phi
   Tri<T> P;
@@ -529,7 +539,7 @@ SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, co
         const T m = Heb[sym_idx(i, j)] + (n[i] * n[j] - ((i == j) ? T(1) : T(0))) * PHb;
         qb[4 + sym_idx(i, j)] = (i == j) ? m : T(2) * m;
       }
-    field_pass<PAIR, T, Acc>(F.phi, F.pr[3], V.base[3], V.basep[3], G, V.t[3], qb, P, xb, acc[3]);
+    field_pass<PAIR, T, AccP>(F.phi, F.pr[3], V.base[3], V.basep[3], G, V.t[3], qb, P, xb, accp);
   }
   const T* g = P.g;
   for (int i = 0; i < 3; ++i) {

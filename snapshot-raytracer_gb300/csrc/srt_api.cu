@@ -118,6 +118,18 @@ struct HostTimer {
 constexpr int64_t kSlabBytes = 512ll << 20;
 
 
+// Device address of host memory the GPU can read directly (pinned and mapped:
+// cudaHostAlloc, or cudaHostRegister with mapping), or NULL.
+const float* mapped_device_pointer(const float* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return (const float*)a.devicePointer;
+}
+
 bool dims_ok(int64_t n0, int64_t n1, int64_t n2) {
   const int64_t lim = int64_t(1) << 20;
   if (n0 < 1 || n1 < 1 || n2 < 1 || n0 > lim || n1 > lim || n2 > lim) return false;
@@ -230,10 +242,26 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
     SRT_CUDA_TRY(pool_alloc((void**)&f->phi, pvox * sizeof(float), s), "allocate phi");
     for (int c = 0; c < 3; ++c) SRT_CUDA_TRY(pool_alloc((void**)&f->b[c], pvox * sizeof(float), s), "allocate B");
     f->bytes = 4 * pvox * (int64_t)sizeof(float);
-    if (dev_in) {
-      SRT_CUDA_TRY(launch_pad_slab(phi, 1, 0, f->phi, f->n, f->pn, 0, n2, s), "pad phi");
-      for (int c = 0; c < 3; ++c)
-        SRT_CUDA_TRY(launch_pad_slab(b_xyz, 3, c, f->b[c], f->n, f->pn, 0, n2, s), "pad B");
+    float* const phi_dst[3] = {f->phi, nullptr, nullptr};
+    // host inputs in mapped pinned memory (cudaHostAlloc / cudaHostRegister)
+    // are read by the layout kernel itself over the host link, with no
+    // staging copy; other host memory streams through a device slab
+    const float* phi_src = phi;
+    const float* b_src = b_xyz;
+    bool direct = dev_in;
+    if (!dev_in && !(flags & SRT_FIELDS_STAGED)) {
+      const float* dp = mapped_device_pointer(phi);
+      const float* db = mapped_device_pointer(b_xyz);
+      if (dp && db) {
+        phi_src = dp;
+        b_src = db;
+        direct = true;
+      }
+    }
+    if (direct) {
+      NvtxRange upload(dev_in ? "layout" : "layout from mapped host memory");
+      SRT_CUDA_TRY(launch_pad_fields(phi_src, 1, phi_dst, f->n, f->pn, 0, n2, s), "pad phi");
+      SRT_CUDA_TRY(launch_pad_fields(b_src, 3, f->b, f->n, f->pn, 0, n2, s), "pad B");
     } else {
       // Stream host planes through one device slab on s: H2D copy, then the
       // pad kernel. (A second slab with the copies on their own stream was
@@ -253,12 +281,8 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
           SRT_CUDA_TRY(cudaMemcpyAsync(slab, src + comps * k0 * plane, comps * (k1 - k0) * plane * sizeof(float),
                                        cudaMemcpyHostToDevice, s),
                        "copy field slab");
-          if (pass == 0) {
-            SRT_CUDA_TRY(launch_pad_slab(slab, 1, 0, f->phi, f->n, f->pn, k0, k1, s), "pad phi");
-          } else {
-            for (int c = 0; c < 3; ++c)
-              SRT_CUDA_TRY(launch_pad_slab(slab, 3, c, f->b[c], f->n, f->pn, k0, k1, s), "pad B");
-          }
+          SRT_CUDA_TRY(launch_pad_fields(slab, comps, pass == 0 ? phi_dst : f->b, f->n, f->pn, k0, k1, s),
+                       pass == 0 ? "pad phi" : "pad B");
         }
       }
     }

@@ -66,8 +66,10 @@ Geom make_geom(const srt_fields* f);
 FieldPtrs make_ptrs(const srt_fields* f);
 
 // Field layout kernels.
-cudaError_t launch_pad_slab(const float* src, int comps, int comp, float* dst, const int64_t n[3],
-                            const int64_t pn[3], int64_t k0, int64_t k1, cudaStream_t s);
+// src: planes k0 .. k1-1 of phi (comps 1, dst[0]) or of the interleaved B
+// (comps 3, dst[0..2]); device memory or mapped pinned host memory.
+cudaError_t launch_pad_fields(const float* src, int comps, float* const dst[3], const int64_t n[3],
+                              const int64_t pn[3], int64_t k0, int64_t k1, cudaStream_t s);
 cudaError_t launch_quantize_half(const float* src, __half* dst, int64_t count, cudaStream_t s);
 cudaError_t launch_pair_build(const float* src, float2* dst, const int64_t pn[3], cudaStream_t s);
 

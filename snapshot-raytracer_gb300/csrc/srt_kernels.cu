@@ -1,6 +1,6 @@
 // srt_kernels.cu — the tracer's device kernels (sm_103a):
-//   * pad_slab_kernel      periodic halo-padded re-layout of a scalar field or
-//                          of one component of the interleaved B field
+//   * pad_fields_kernel    periodic halo-padded re-layout of the scalar phi or
+//                          of the interleaved B field (every source voxel read once)
 //                          (replaces vector3_to_half, snapshot-raytracer.cu:585-597,
 //                          and the staged uploads of :774-844)
 //   * quantize_half_kernel half(B * 2^27) planes for the REF16 mode
@@ -18,40 +18,77 @@ namespace srt {
 
 // ------------------------------------------------------------- field layout
 
-// Destination padded plane `pk` for source plane `k`, slot 0..3:
-// pk = k + 1; 0 when k is the last plane; n2 + 1 when k == 0; n2 + 2 when
-// k == 1 mod n2. Returns -1 when the slot does not apply.
-__device__ __forceinline__ int64_t dest_plane(int64_t k, int slot, int64_t n2) {
-  switch (slot) {
-    case 0: return k + 1;
-    case 1: return (k == n2 - 1) ? 0 : -1;
-    case 2: return (k == 0) ? n2 + 1 : -1;
-    default: return (k == (1 % n2)) ? n2 + 2 : -1;
+// Padded coordinates of source coordinate c on an axis of extent n: padded
+// coordinate q holds voxel (q - 1) mod n for q in [0, n + 3), so c appears at
+// c + 1 and, near the ends, in the halo (n - 1 -> 0, 0 -> n + 1, 1 -> n + 2).
+// Returns how many of out[0..3] it filled.
+__device__ __forceinline__ int padded_coords(int64_t c, int64_t n, int64_t out[4]) {
+  int m = 0;
+  out[m++] = c + 1;
+  if (c == n - 1) out[m++] = 0;
+  if (c == 0) out[m++] = n + 1;
+  if (c == 1 % n) out[m++] = n + 2;
+  return m;
+}
+
+// One thread per source voxel of planes k0 .. k1-1 (x fastest, `comps` floats
+// per voxel: 1 for phi, 3 for the interleaved B), each source byte read once
+// and in 16-byte pieces where it is aligned, so this kernel can read the
+// source straight from mapped pinned host memory over the host link: a block's
+// 256 B voxels (3 KB) are loaded as 192 float4 into shared memory and then
+// picked per thread. Component c goes to padded plane array dst[c] at every
+// padded position of the voxel (its interior one and its periodic halo
+// copies). Replaces vector3_to_half (snapshot-raytracer.cu:585-597) and the
+// staged uploads of :774-844. grid: x over a plane, y over planes.
+constexpr int kPadThreads = 256;
+
+__global__ void __launch_bounds__(kPadThreads) pad_fields_kernel(const float* __restrict__ src, int comps,
+                                                                  float* __restrict__ d0, float* __restrict__ d1,
+                                                                  float* __restrict__ d2, int64_t n0, int64_t n1,
+                                                                  int64_t n2, int64_t p0, int64_t p1, int64_t k0) {
+  __shared__ float4 stage[kPadThreads * 3 / 4];
+  const int64_t plane = n0 * n1;
+  const int64_t q0 = (int64_t)blockIdx.x * kPadThreads;  // first voxel of the block in its plane
+  const int64_t q = q0 + threadIdx.x;
+  const int64_t kl = blockIdx.y;  // plane within the launch
+  const int64_t v = kl * plane + q;
+  float val[3];
+  if (comps == 3) {
+    const float* blk = src + (kl * plane + q0) * 3;
+    const int64_t nv = plane - q0 < kPadThreads ? plane - q0 : kPadThreads;  // voxels of this block
+    if (nv == kPadThreads && ((uintptr_t)blk & 15) == 0) {
+      // whole block, aligned: 192 float4 loads cover its 768 floats
+      if (threadIdx.x < kPadThreads * 3 / 4) stage[threadIdx.x] = reinterpret_cast<const float4*>(blk)[threadIdx.x];
+      __syncthreads();
+      const float* st = reinterpret_cast<const float*>(stage);
+      for (int c = 0; c < 3; ++c) val[c] = st[3 * threadIdx.x + c];
+    } else if (q < plane) {
+      for (int c = 0; c < 3; ++c) val[c] = src[v * 3 + c];
+    }
+  } else if (q < plane) {
+    val[0] = src[v];
   }
+  if (q >= plane) return;
+  const int64_t i = q % n0, j = q / n0, k = k0 + kl;
+  int64_t pi[4], pj[4], pk[4];
+  const int ni = padded_coords(i, n0, pi), nj = padded_coords(j, n1, pj), nk = padded_coords(k, n2, pk);
+  float* const dst[3] = {d0, d1, d2};
+  for (int a = 0; a < nk; ++a)
+    for (int b = 0; b < nj; ++b)
+      for (int c = 0; c < ni; ++c) {
+        const int64_t o = pi[c] + p0 * (pj[b] + p1 * pk[a]);
+        for (int comp = 0; comp < comps; ++comp) dst[comp][o] = val[comp];
+      }
 }
 
-// src holds source planes k0 .. k1-1 (x fastest), `comps` floats per voxel.
-__global__ void pad_slab_kernel(const float* __restrict__ src, int comps, int comp,
-                                float* __restrict__ dst, int64_t n0, int64_t n1, int64_t n2,
-                                int64_t p0, int64_t p1, int64_t k0) {
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // index in a padded plane
-  if (q >= p0 * p1) return;
-  const int64_t k = k0 + blockIdx.y;
-  const int64_t pk = dest_plane(k, (int)blockIdx.z, n2);
-  if (pk < 0) return;
-  const int64_t pi = q % p0, pj = q / p0;
-  const int64_t i = (pi - 1 + n0) % n0, j = (pj - 1 + n1) % n1;
-  dst[q + p0 * p1 * pk] = src[(((k - k0) * n1 + j) * n0 + i) * comps + comp];
-}
-
-cudaError_t launch_pad_slab(const float* src, int comps, int comp, float* dst, const int64_t n[3],
-                            const int64_t pn[3], int64_t k0, int64_t k1, cudaStream_t s) {
-  const int64_t plane = pn[0] * pn[1];
+cudaError_t launch_pad_fields(const float* src, int comps, float* const dst[3], const int64_t n[3],
+                              const int64_t pn[3], int64_t k0, int64_t k1, cudaStream_t s) {
+  const int64_t plane = n[0] * n[1];
   for (int64_t kb = k0; kb < k1; kb += 65535) {
     const int64_t ke = kb + 65535 < k1 ? kb + 65535 : k1;
-    dim3 grid((unsigned)((plane + 255) / 256), (unsigned)(ke - kb), 4);
-    pad_slab_kernel<<<grid, 256, 0, s>>>(src + (kb - k0) * n[0] * n[1] * comps, comps, comp, dst, n[0],
-                                         n[1], n[2], pn[0], pn[1], kb);
+    dim3 grid((unsigned)((plane + kPadThreads - 1) / kPadThreads), (unsigned)(ke - kb), 1);
+    pad_fields_kernel<<<grid, kPadThreads, 0, s>>>(src + (kb - k0) * plane * comps, comps, dst[0], dst[1], dst[2], n[0],
+                                           n[1], n[2], pn[0], pn[1], kb);
   }
   return cudaGetLastError();
 }

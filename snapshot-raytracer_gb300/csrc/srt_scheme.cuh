@@ -191,11 +191,15 @@ SRT_HD void tri_scale(Tri<T>& r, T s) {
 #if defined(__CUDA_ARCH__)
 SRT_HD float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 SRT_HD float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+SRT_HD float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 #else
 SRT_HD float2 ffma2(float2 a, float2 b, float2 c) { return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y)); }
 SRT_HD float2 fmul2(float2 a, float2 b) { return make_float2(a.x * b.x, a.y * b.y); }
+SRT_HD float2 fadd2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 #endif
 SRT_HD float2 dup2(float v) { return make_float2(v, v); }
+// a - b, one rounding (there is no packed subtract: -1 * b + a)
+SRT_HD float2 fsub2(float2 a, float2 b) { return ffma2(dup2(-1.f), b, a); }
 
 // Where the packed passes get their taps: rows y and y+1 of a slice, tap i,
 // as one float2. Two sources:
@@ -220,10 +224,14 @@ struct SingleRows {
   }
 };
 
-// The same interpolation as `tricubic` with every pass on packed pairs (two
-// FP32 FMAs per instruction): the x pass on rows y and y+1 at once with
-// duplicated x weights, the y pass with the weights of rows (0, 1) and
-// (2, 3), the z pass on even/odd partial sums that are added at the end.
+// The same interpolation as `tricubic` on packed pairs (two FP32 FMAs per
+// instruction): the x pass on rows y and y+1 at once with duplicated x
+// weights, the y pass with the weights of rows (0, 1) and (2, 3) (even / odd
+// partial sums). Per slice the six y sums are then completed (one add each)
+// and the z pass forms the ten outputs as five pairs that share an operand
+// pair: (v, gx) and (gz, hxz) from (a, ax), (hzz, gy) from (a, ay),
+// (hyz, hyy) from (ay, ayy), (hxx, hxy) from (axx, axy), so no lane of the
+// z pass is idle.
 template <typename Rows>
 SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float>& Y, const CRW<float>& Z,
                           Tri<float>& r) {
@@ -237,7 +245,8 @@ SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float
   const float2 yg[2] = {make_float2(Y.g[0], Y.g[1]), make_float2(Y.g[2], Y.g[3])};
   const float2 yh[2] = {make_float2(Y.h[0], Y.h[1]), make_float2(Y.h[2], Y.h[3])};
   const float2 z0 = make_float2(0.f, 0.f);
-  float2 V = z0, G0 = z0, G1 = z0, G2 = z0, H00 = z0, H01 = z0, H02 = z0, H11 = z0, H12 = z0, H22 = z0;
+  // z-pass accumulators: (v, gx), (gz, hxz), (hzz, gy), (hyz, hyy), (hxx, hxy)
+  float2 VG0 = z0, G2H02 = z0, H22G1 = z0, H12H11 = z0, H00H01 = z0;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float2 A = z0, AY = z0, AYY = z0, AX = z0, AXY = z0, AXX = z0;
@@ -261,28 +270,25 @@ SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float
       AXY = ffma2(yg[pr], RX, AXY);
       AXX = ffma2(yw[pr], RXX, AXX);
     }
-    const float2 zw = dup2(Z.w[c]), zg = dup2(Z.g[c]), zh = dup2(Z.h[c]);
-    V = ffma2(zw, A, V);
-    G0 = ffma2(zw, AX, G0);
-    G1 = ffma2(zw, AY, G1);
-    G2 = ffma2(zg, A, G2);
-    H00 = ffma2(zw, AXX, H00);
-    H01 = ffma2(zw, AXY, H01);
-    H02 = ffma2(zg, AX, H02);
-    H11 = ffma2(zw, AYY, H11);
-    H12 = ffma2(zg, AY, H12);
-    H22 = ffma2(zh, A, H22);
+    const float a = A.x + A.y, ax = AX.x + AX.y, ay = AY.x + AY.y;
+    const float axx = AXX.x + AXX.y, axy = AXY.x + AXY.y, ayy = AYY.x + AYY.y;
+    const float zw = Z.w[c], zg = Z.g[c], zh = Z.h[c];
+    VG0 = ffma2(dup2(zw), make_float2(a, ax), VG0);
+    G2H02 = ffma2(dup2(zg), make_float2(a, ax), G2H02);
+    H22G1 = ffma2(make_float2(zh, zw), make_float2(a, ay), H22G1);
+    H12H11 = ffma2(make_float2(zg, zw), make_float2(ay, ayy), H12H11);
+    H00H01 = ffma2(dup2(zw), make_float2(axx, axy), H00H01);
   }
-  r.v = V.x + V.y;
-  r.g[0] = G0.x + G0.y;
-  r.g[1] = G1.x + G1.y;
-  r.g[2] = G2.x + G2.y;
-  r.h[0] = H00.x + H00.y;
-  r.h[1] = H01.x + H01.y;
-  r.h[2] = H02.x + H02.y;
-  r.h[3] = H11.x + H11.y;
-  r.h[4] = H12.x + H12.y;
-  r.h[5] = H22.x + H22.y;
+  r.v = VG0.x;
+  r.g[0] = VG0.y;
+  r.g[1] = H22G1.y;
+  r.g[2] = G2H02.x;
+  r.h[0] = H00H01.x;
+  r.h[1] = H00H01.y;
+  r.h[2] = G2H02.y;
+  r.h[3] = H12H11.y;
+  r.h[4] = H12H11.x;
+  r.h[5] = H22G1.x;
 }
 
 // ------------------------------------------------------------ cell lookup
@@ -988,10 +994,19 @@ SRT_HD void init_mixed(const RayDir& d, MixedRay& R, float* y) {
   for (int j = 12; j < kMixedState; ++j) y[j] = 0.f;
 }
 
-// Stage input y + c k of the perturbation state (compensations folded in).
+// Stage input y + c k of the perturbation state (compensations folded in),
+// two components per packed instruction.
 SRT_HD void mixed_stage(const float* y, const float* k, float c, float* ys) {
-  for (int j = 0; j < kCompensated; ++j) ys[j] = y[j] + (y[19 + j] + c * k[j]);
-  for (int j = kCompensated; j < 19; ++j) ys[j] = y[j] + c * k[j];
+  static_assert(kCompensated == 19, "packed stage assumes every component is compensated");
+  const float2 c2 = dup2(c);
+#pragma unroll
+  for (int j = 0; j < 18; j += 2) {
+    const float2 r = fadd2(make_float2(y[j], y[j + 1]),
+                           ffma2(c2, make_float2(k[j], k[j + 1]), make_float2(y[19 + j], y[20 + j])));
+    ys[j] = r.x;
+    ys[j + 1] = r.y;
+  }
+  ys[18] = y[18] + (y[37] + c * k[18]);
 }
 
 // One RK4 step from affine parameter `step`; when us is given, the four stage
@@ -1015,15 +1030,39 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
     // at s = 0 the ray sits exactly on the observer (a grid node, offsets
     // exactly 0) in both precisions, so no cell choice can differ there
     if (step == 0 && st == 0 && gd.m) gd.m[1] = 1.f;
-    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
+    if (st == 0) {
+      for (int j = 0; j < 19; ++j) acc[j] = k[j];
+    } else if (st < 3) {
+#pragma unroll
+      for (int j = 0; j < 18; j += 2) {
+        const float2 r = ffma2(dup2(2.f), make_float2(k[j], k[j + 1]), make_float2(acc[j], acc[j + 1]));
+        acc[j] = r.x;
+        acc[j + 1] = r.y;
+      }
+      acc[18] += 2.f * k[18];
+    }
   }
-  for (int j = 0; j < kCompensated; ++j) {
+  // y += (k1 + 2 k2 + 2 k3 + k4) / 6 with the rounding error of each sum kept
+  // in the compensation (two-sum), two components per packed instruction
+#pragma unroll
+  for (int j = 0; j < 18; j += 2) {
+    const float2 a = make_float2(y[j], y[j + 1]);
+    const float2 b = fmul2(fadd2(make_float2(acc[j], acc[j + 1]), make_float2(k[j], k[j + 1])), dup2(1.f / 6.f));
+    const float2 sm = fadd2(a, b);  // two-sum: sm + e = a + b exactly
+    const float2 bb = fsub2(sm, a);
+    const float2 e = fadd2(fsub2(a, fsub2(sm, bb)), fsub2(b, bb));
+    const float2 yc = fadd2(make_float2(y[19 + j], y[20 + j]), e);
+    y[j] = sm.x;
+    y[j + 1] = sm.y;
+    y[19 + j] = yc.x;
+    y[20 + j] = yc.y;
+  }
+  {
     float sum, err;
-    two_sum(y[j], (acc[j] + k[j]) * (1.f / 6.f), sum, err);
-    y[j] = sum;
-    y[19 + j] += err;
+    two_sum(y[18], (acc[18] + k[18]) * (1.f / 6.f), sum, err);
+    y[18] = sum;
+    y[37] += err;
   }
-  for (int j = kCompensated; j < 19; ++j) y[j] += (acc[j] + k[j]) * (1.f / 6.f);
 }
 
 // Extraction in FP32 on the perturbation: the displacement is

@@ -28,6 +28,7 @@ SRT_DETERMINISTIC = 16
 SRT_FIELDS_NO_PAIRS = 32
 SRT_MIXED_NO_REFINE = 64
 SRT_NESTED_RANGE = 128
+SRT_FIELDS_STAGED = 256
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
           -5: "format error", -6: "no CUDA device", -7: "unsupported", -8: "overflow"}
@@ -166,9 +167,11 @@ def _stream_ptr(stream):
 
 class Fields:
     """Laid-out phi and B on the GPU (srt_fields_create). phi: (n2, n1, n0)
-    float32; b_xyz: (n2, n1, n0, 3) float32; numpy (host) or CUDA tensors."""
+    float32; b_xyz: (n2, n1, n0, 3) float32; numpy (host) or CUDA tensors.
+    Host arrays in pinned memory are read by the layout kernel directly unless
+    staged=True (copied through a device slab, as pageable memory is)."""
 
-    def __init__(self, phi, b_xyz, stream=None, async_=False, pairs=True):
+    def __init__(self, phi, b_xyz, stream=None, async_=False, pairs=True, staged=False):
         shape = tuple(phi.shape)
         if len(shape) != 3 or tuple(b_xyz.shape) != shape + (3,):
             raise ValueError("phi must be (n2, n1, n0) and b_xyz (n2, n1, n0, 3); got %r and %r"
@@ -182,7 +185,7 @@ class Fields:
             raise ValueError("phi and b_xyz must both be on the host or both on the device")
         self.n = (shape[2], shape[1], shape[0])
         flags = (SRT_INPUT_DEVICE if dev_phi else 0) | (SRT_ASYNC if async_ else 0) | \
-            (0 if pairs else SRT_FIELDS_NO_PAIRS)
+            (0 if pairs else SRT_FIELDS_NO_PAIRS) | (SRT_FIELDS_STAGED if staged else 0)
         h = _P()
         _check(lib().srt_fields_create(p_phi, p_b, self.n[0], self.n[1], self.n[2], flags, _stream_ptr(stream),
                                        ctypes.byref(h)))

@@ -48,7 +48,7 @@ void rhs_vjp_fp64(const double* y, const double* fb, double* yb, double* gbx, do
   acc[1].g = gby;
   acc[2].g = gbz;
   acc[3].g = gphi;
-  srt::rhs_vjp<double, srt::AccF64, false>(V, ptrs(phi, bx, by, bz), G, fb, yb, acc);
+  srt::rhs_vjp<double, srt::AccF64, srt::AccF64, false>(V, ptrs(phi, bx, by, bz), G, fb, yb, acc, acc[3]);
 }
 
 // Index audit of the MIXED sweep (rhs_vjp<float> on stage_view_mixed, as
@@ -94,7 +94,7 @@ void audit_vjp_indices_mixed(int n0, int n1, int n2, int count, const double* th
       fb[j] = 1.f;
       yb[j] = 0.f;
     }
-    srt::rhs_vjp<float, AccAudit, false>(V, F, G, fb, yb, acc);
+    srt::rhs_vjp<float, AccAudit, AccAudit, false>(V, F, G, fb, yb, acc, acc[3]);
     for (int f = 0; f < 4; ++f) {
       // the PAIR pass reads pair basep + c pxy2 + 2 pr px + i (c <= 3, pr <= 1, i <= 3)
       const int64_t last = V.basep[f] + 3 * G.pxy2 + 2 * G.px + 3;

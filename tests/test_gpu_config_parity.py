@@ -24,14 +24,15 @@ pytestmark = pytest.mark.gpu
 N, NSIDE, STEPS, BATCH, SEED = 128, 32, 64, 0, 128
 BEGIN, COUNT = BATCH * NSIDE * NSIDE, NSIDE * NSIDE
 
-# (rms, max) bounds per comparison
+# (rms, max) bounds per comparison, a few times the errors measured on a GB300
+# (in brackets: the largest rms and max over the six maps)
 BOUNDS = {
-    "fp64_vs_oracle": (1e-6, 1e-5),      # same FP64 scheme; FMA contraction differs (~1e-16)
-    "mixed_vs_oracle": (2e-6, 2e-5),     # the MIXED target is rms <= 1e-5
-    "ref16_vs_oracle": (2e-3, 1e-1),     # FP16 B planes and FP32 cell offsets of the reference
-    "refgpu_vs_oracle": (2e-3, 1e-1),
-    "refgpu_vs_fp64": (2e-3, 1e-1),
-    "refgpu_vs_ref16": (2e-5, 2e-3),     # same arithmetic, --use_fast_math rounding order
+    "fp64_vs_oracle": (1e-8, 1e-7),      # the same FP64 scheme: identical floats [0, 0]
+    "mixed_vs_oracle": (5e-7, 3e-6),     # [1.3e-7, 7.5e-7]; the MIXED target is rms <= 1e-5
+    "ref16_vs_oracle": (2e-5, 1e-4),     # the reference's FP16 B planes, FP32 cell offsets [5.3e-6, 2.8e-5]
+    "refgpu_vs_oracle": (2e-5, 4e-4),    # [5.3e-6, 1.1e-4]
+    "refgpu_vs_fp64": (2e-5, 4e-4),      # [5.3e-6, 1.1e-4]
+    "refgpu_vs_ref16": (1.5e-5, 4e-4),   # same arithmetic, --use_fast_math rounding order [3.5e-6, 1.1e-4]
 }
 
 

@@ -277,9 +277,13 @@ def test_constant_gradient_potential_analytic(srt, orc, precision):
 def test_single_layout_packed_path_equals_pair_layout(srt):
     """The MIXED forward and vjp read their packed tap pairs either from the
     row-pair copy of the fields or, with SRT_FIELDS_NO_PAIRS, from the single
-    halo layout (two loads per pair): the float2 values and every operation
-    are the same, so the maps, the refined-ray counts and the deterministic
-    gradients agree bit for bit."""
+    halo layout (two loads per pair): the float2 values and the packed
+    operations are the same, so the maps, the refined-ray counts and the
+    deterministic phi gradient agree bit for bit. The B components' tap
+    cotangents come from scalar FP32 expressions the compiler may round in a
+    different order in the two kernel variants: measured one float ulp on
+    ~0.5 % of the B gradient entries, so those are compared to 1e-6 of the
+    largest entry."""
     import srt_fields
 
     phi, b = srt_fields.gaussian_fields_np(48, seed=17)
@@ -294,4 +298,34 @@ def test_single_layout_packed_path_equals_pair_layout(srt):
     assert np.array_equal(out[True][0].view(np.uint32), out[False][0].view(np.uint32))
     assert out[True][1] == out[False][1]
     assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
-    assert np.array_equal(out[True][3].view(np.uint32), out[False][3].view(np.uint32))
+    gb_p, gb_s = out[True][3], out[False][3]
+    assert np.abs(gb_p - gb_s).max() <= 1e-6 * np.abs(gb_p).max()
+
+
+@pytest.mark.parametrize("extents", [(24, 24, 24), (5, 3, 4)])
+def test_pinned_host_inputs_read_in_place_equal_staged(srt, orc, extents):
+    """Host fields in pinned (mapped) memory are laid out by the kernel reading
+    them over the host link; pageable ones, or pinned ones with
+    SRT_FIELDS_STAGED, go through a device slab. All three give the same
+    padded fields: the FP64 maps agree bit for bit with each other and with the
+    oracle, on a cube and on a small non-cubic grid whose rays wrap around the
+    box many times (every halo copy is read)."""
+    torch = pytest.importorskip("torch")
+    import srt_fields
+
+    phi, b = srt_fields.int_noise_fields(extents, seed=8)
+    pphi = torch.empty(phi.shape, dtype=torch.float32, pin_memory=True)
+    pb = torch.empty(b.shape, dtype=torch.float32, pin_memory=True)
+    pphi.numpy()[...] = phi
+    pb.numpy()[...] = b
+    nside, steps = 2, 20
+    want = orc.trace(phi, b, nside, steps, mode="fp64")
+    got = []
+    for src, staged in ((pphi.numpy(), False), (pphi.numpy(), True), (phi, False)):
+        bsrc = pb.numpy() if src is not phi else b
+        with srt.Fields(src, bsrc, staged=staged) as f:
+            got.append(f.forward(nside, steps, precision="fp64")[0])
+    for g in got:
+        assert np.array_equal(g.view(np.uint32), got[0].view(np.uint32))
+    for m, (rms, mx) in enumerate(map_errors(got[0], want)):
+        assert rms <= 1e-9 and mx <= 1e-8, (m, rms, mx)

@@ -60,6 +60,10 @@ def test_reference_build_gaussian(srt, refgpu):
     for m in range(6):
         # same arithmetic with a different FP32 rounding order (the reference is
         # built with --use_fast_math): measured 1.2e-4 rms at most (dA)
-        assert e16[m][0] <= 1e-3, "ref GPU vs REF16 map %d rms %.3g" % (m, e16[m][0])
-        # the reference's FP16 B planes and FP32 cell offsets cost it accuracy
-        assert e64[m][0] <= 1e-2, "ref GPU vs FP64 map %d rms %.3g" % (m, e64[m][0])
+        assert e16[m][0] <= 5e-4, "ref GPU vs REF16 map %d rms %.3g" % (m, e16[m][0])
+        # the reference's FP16 B planes and FP32 cell offsets cost it accuracy:
+        # at 128^3 / nside 32 / 64 steps the measured envelope is 5.3e-6 rms and
+        # 1.1e-4 max over the maps (tests/test_gpu_config_parity.py), at
+        # 512^3 / nside 256 / 256 steps 1.3e-4 rms and 3.5e-2 max
+        assert e64[m][0] <= 5e-4 and e64[m][1] <= 5e-2, "ref GPU vs FP64 map %d rms %.3g max %.3g" % (
+            m, e64[m][0], e64[m][1])
