@@ -53,6 +53,8 @@ extern "C" {
 #define SRT_ERR_UNSUPPORTED (-7)
 #define SRT_ERR_OVERFLOW (-8) /* srt_vjp, SRT_DETERMINISTIC: a gradient beyond the
                                  fixed-point range */
+#define SRT_ERR_CANCELLED (-9) /* srt_fields_load_h5: the progress callback asked
+                                  to stop */
 
 /* precision modes of srt_forward / srt_vjp */
 #define SRT_PRECISION_FP64 0  /* all-FP64 interpolation, right-hand side and state */
@@ -134,6 +136,47 @@ int srt_device_count(void);
  * staged vector3_to_half passes and the phi copy). */
 int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t n1,
                       int64_t n2, unsigned flags, void* stream, srt_fields** out);
+
+/* Progress of srt_fields_load_h5, reported on the calling thread in this order
+ * (dims: the extents of the dataset concerned, in file order). The callback
+ * returns 0 to go on; anything else stops the load, which then releases what
+ * it holds and returns SRT_ERR_CANCELLED. */
+#define SRT_LOAD_PHI_DIMS 1 /* phi's header is read; its data are being read */
+#define SRT_LOAD_B_START 2  /* phi is read; the B file's data are being read */
+#define SRT_LOAD_B_DIMS 3   /* B's extents (checked against phi's) */
+#define SRT_LOAD_UPLOAD 4   /* both files are read; the last planes are being laid out */
+typedef int (*srt_load_progress)(int event, const int64_t dims[3], void* ctx);
+
+#define SRT_LOAD_XYZ_HDF5 512u /* srt_fields_load_h5: x is the fastest (last)
+                                  HDF5 axis with its own extent; by default the
+                                  extents are taken in file order, as the
+                                  reference does */
+
+typedef struct srt_load_stats {
+  double read_phi_ms;   /* reading (and converting) phi's data, reader thread */
+  double read_b_ms;     /* the same for B */
+  double layout_ms;     /* host->device copies and layout, overlapped with the reads */
+  double after_read_ms; /* from the end of the reads to the fields being ready */
+  double total_ms;      /* wall time of the call */
+  int64_t h2d_bytes;    /* bytes copied host -> device */
+  int64_t n[3];         /* grid extents of the handle, fastest first (n0, n1, n2) */
+} srt_load_stats;
+
+/* Read dataset `dset` of the potential file and of the B file (any float or
+ * integer element type for phi, array[3] of float for B, with the checks of
+ * srt_h5_read_scalar / srt_h5_read_vector3) and lay them out on the device
+ * while they are read: a reader thread fills host memory in file order, and
+ * every run of planes is copied and laid out as soon as it is complete, so the
+ * upload overlaps the read. phi_scale / b_scale multiply the values (1: as
+ * read). flags: SRT_LOAD_XYZ_HDF5, SRT_FIELDS_NO_PAIRS. progress (may be NULL)
+ * reports the steps the reference prints. Without a CUDA device both files are
+ * still read and checked (file errors first, as the reference reports them)
+ * before SRT_ERR_NO_DEVICE. Replaces snapshot-raytracer.cu:640
+ * and :676 (load_hdf5_array, load_hdf5_vector_field) followed by :752-855
+ * (device allocation and the staged copies). */
+int srt_fields_load_h5(const char* phi_path, const char* b_path, const char* dset, unsigned flags,
+                       double phi_scale, double b_scale, srt_load_progress progress, void* ctx,
+                       srt_fields** out, srt_load_stats* stats);
 
 /* Release the device memory of a fields handle (NULL is a no-op). Replaces
  * the reference's cudaFree calls (snapshot-raytracer.cu:917-920, :993-998). */

@@ -2,12 +2,14 @@
 // and layout, the forward trace, HEALPix helpers and error reporting.
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <thread>
 #include "srt_internal.h"
 
 namespace {
@@ -215,6 +217,57 @@ int srt_device_count(void) {
   return n;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Row-pair arrays for the packed MIXED path, when they fit with room to spare
+// (unless SRT_FIELDS_NO_PAIRS).
+int build_row_pairs(srt_fields* f, unsigned flags, cudaStream_t s) {
+  if (flags & SRT_FIELDS_NO_PAIRS) return SRT_OK;
+  const int64_t pair_bytes = 4 * f->pn[0] * (f->pn[1] - 1) * f->pn[2] * (int64_t)sizeof(float2);
+  size_t free_b = 0, total_b = 0;
+  const bool have = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess;
+  const int64_t avail = (int64_t)free_b + pool_reusable_bytes(f->device);
+  if (!have || pair_bytes + (int64_t(4) << 30) >= avail) return SRT_OK;
+  const float* srcs[4] = {f->b[0], f->b[1], f->b[2], f->phi};
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < 4 && e == cudaSuccess; ++c) {
+    e = pool_alloc((void**)&f->pr[c], pair_bytes / 4, s);
+    if (e != cudaSuccess) return cuda_error(e, "allocate row pairs");
+    e = launch_pair_build(srcs[c], f->pr[c], f->pn, s);
+  }
+  if (e != cudaSuccess) return cuda_error(e, "row pairs");
+  f->bytes += pair_bytes;
+  if (!(flags & SRT_ASYNC)) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_error(e, "row pairs");
+  }
+  return SRT_OK;
+}
+
+// Device arrays of the laid-out fields of an n0 x n1 x n2 grid (no contents).
+int alloc_fields(srt_fields* f, int64_t n0, int64_t n1, int64_t n2, cudaStream_t s) {
+  cudaGetDevice(&f->device);
+  for (int i = 0; i < 3; ++i) {
+    f->n[i] = (i == 0 ? n0 : (i == 1 ? n1 : n2));
+    f->pn[i] = f->n[i] + 3;
+  }
+  const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
+  cudaError_t e = pool_alloc((void**)&f->phi, pvox * sizeof(float), s);
+  if (e != cudaSuccess) return cuda_error(e, "allocate phi");
+  for (int c = 0; c < 3; ++c) {
+    e = pool_alloc((void**)&f->b[c], pvox * sizeof(float), s);
+    if (e != cudaSuccess) return cuda_error(e, "allocate B");
+  }
+  f->bytes = 4 * pvox * (int64_t)sizeof(float);
+  return SRT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t n1, int64_t n2,
                       unsigned flags, void* stream, srt_fields** out) {
   NvtxRange nvtx_("srt_fields_create");
@@ -239,6 +292,7 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
     }
     const int64_t pvox = f->pn[0] * f->pn[1] * f->pn[2];
     const int64_t plane = n0 * n1;
+    const int64_t vox = plane * n2;
     SRT_CUDA_TRY(pool_alloc((void**)&f->phi, pvox * sizeof(float), s), "allocate phi");
     for (int c = 0; c < 3; ++c) SRT_CUDA_TRY(pool_alloc((void**)&f->b[c], pvox * sizeof(float), s), "allocate B");
     f->bytes = 4 * pvox * (int64_t)sizeof(float);
@@ -262,7 +316,18 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
       NvtxRange upload(dev_in ? "layout" : "layout from mapped host memory");
       SRT_CUDA_TRY(launch_pad_fields(phi_src, 1, phi_dst, f->n, f->pn, 0, n2, s), "pad phi");
       SRT_CUDA_TRY(launch_pad_fields(b_src, 3, f->b, f->n, f->pn, 0, n2, s), "pad B");
+    } else if ((flags & SRT_ASYNC) && pool_alloc((void**)&slab, 4 * vox * sizeof(float), s) == cudaSuccess) {
+      // asynchronous: the whole input through one staging buffer, so the
+      // copy engines move it without waiting for a layout kernel between
+      // slabs (those would wait for SM slots while other work runs), then
+      // one layout kernel per field
+      NvtxRange upload("upload (one staging buffer) and layout");
+      SRT_CUDA_TRY(cudaMemcpyAsync(slab, phi, vox * sizeof(float), cudaMemcpyHostToDevice, s), "copy phi");
+      SRT_CUDA_TRY(cudaMemcpyAsync(slab + vox, b_xyz, 3 * vox * sizeof(float), cudaMemcpyHostToDevice, s), "copy B");
+      SRT_CUDA_TRY(launch_pad_fields(slab, 1, phi_dst, f->n, f->pn, 0, n2, s), "pad phi");
+      SRT_CUDA_TRY(launch_pad_fields(slab + vox, 3, f->b, f->n, f->pn, 0, n2, s), "pad B");
     } else {
+      cudaGetLastError();  // a failed whole-input staging allocation falls back to slabs
       // Stream host planes through one device slab on s: H2D copy, then the
       // pad kernel. (A second slab with the copies on their own stream was
       // measured slower in steady use: 250-310 ms against 190-210 ms for the
@@ -286,25 +351,11 @@ int srt_fields_create(const float* phi, const float* b_xyz, int64_t n0, int64_t 
         }
       }
     }
-    if (!(flags & SRT_ASYNC) || slab) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
-    pool_free(slab, s);  // after the last pad kernel on s
+    if (!(flags & SRT_ASYNC)) SRT_CUDA_TRY(cudaStreamSynchronize(s), "field layout");
+    pool_free(slab, s);  // stream-ordered: after the last pad kernel on s
     slab = nullptr;
-    if (!(flags & SRT_FIELDS_NO_PAIRS)) {
-      // row-pair arrays for the packed MIXED path, when they fit with room to spare
-      const int64_t pair_bytes = 4 * f->pn[0] * (f->pn[1] - 1) * f->pn[2] * (int64_t)sizeof(float2);
-      size_t free_b = 0, total_b = 0;
-      const bool have = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess;
-      const int64_t avail = (int64_t)free_b + pool_reusable_bytes(f->device);
-      if (have && pair_bytes + (int64_t(4) << 30) < avail) {
-        const float* srcs[4] = {f->b[0], f->b[1], f->b[2], f->phi};
-        for (int c = 0; c < 4; ++c) {
-          SRT_CUDA_TRY(pool_alloc((void**)&f->pr[c], pair_bytes / 4, s), "allocate row pairs");
-          SRT_CUDA_TRY(launch_pair_build(srcs[c], f->pr[c], f->pn, s), "row pairs");
-        }
-        f->bytes += pair_bytes;
-        if (!(flags & SRT_ASYNC)) SRT_CUDA_TRY(cudaStreamSynchronize(s), "row pairs");
-      }
-    }
+    rc = build_row_pairs(f, flags, s);
+    if (rc != SRT_OK) goto fail;
   }
   *out = f;
   return SRT_OK;
@@ -440,7 +491,9 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     if (dev_out) {
       for (int m = 0; m < 6; ++m) a.maps[m] = maps[m];
     } else {
-      SRT_CUDA_TRY(dev_alloc((void**)&dmaps, 6 * pix_count * sizeof(float)), "cudaMalloc(maps)");
+      // stream-ordered: a plain device allocation issued here would keep this
+      // trace from running beside work already queued on other streams
+      SRT_CUDA_TRY(dev_alloc_async((void**)&dmaps, 6 * pix_count * sizeof(float), s), "cudaMallocAsync(maps)");
       for (int m = 0; m < 6; ++m) a.maps[m] = dmaps + m * pix_count;
     }
     const bool timed = !(flags & SRT_ASYNC);
@@ -475,7 +528,7 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     }
   }
 fail:
-  if (dmaps) cudaFree(dmaps);
+  if (dmaps) cudaFreeAsync(dmaps, s);
   // stream-ordered release: the refine kernel may still be queued (SRT_ASYNC)
   if (refine_list) cudaFreeAsync(refine_list, s);
   if (refine_count) cudaFreeAsync(refine_count, s);
@@ -484,6 +537,251 @@ fail:
   if (prev != f->device) cudaSetDevice(prev);
   if (stats) stats->total_ms = wall.ms();
   return rc;
+}
+
+int srt_fields_load_h5(const char* phi_path, const char* b_path, const char* dset, unsigned flags, double phi_scale,
+                       double b_scale, srt_load_progress progress, void* ctx, srt_fields** out,
+                       srt_load_stats* stats) {
+  NvtxRange nvtx_("srt_fields_load_h5");
+  const auto t_start = std::chrono::steady_clock::now();
+  auto ms_since = [&](std::chrono::steady_clock::time_point t) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+  };
+  if (!out) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_load_h5: out is NULL");
+  *out = nullptr;
+  if (!phi_path || !b_path || !dset) return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_load_h5: NULL path");
+  if (stats) memset(stats, 0, sizeof(*stats));
+  // ---- phi's header (the extents); file errors come before device errors,
+  // as in the reference, which reads its files before touching the device
+  H5Field* hphi = nullptr;
+  int64_t pd[8] = {0};
+  int prank = 0;
+  int rc = h5_field_open(phi_path, dset, false, pd, &prank, &hphi);
+  if (rc != SRT_OK) return rc;
+  if (prank < 3) {
+    h5_field_close(hphi);
+    return set_error(SRT_ERR_FORMAT, "Expected a 3D potential dataset, got rank=%d", prank);
+  }
+  // grid extents, fastest first: the reference takes the HDF5 extents in file
+  // order (snapshot-raytracer.cu:645), SRT_LOAD_XYZ_HDF5 the fastest axis first
+  const bool hdf5_order = (flags & SRT_LOAD_XYZ_HDF5) != 0;
+  const int64_t n0 = hdf5_order ? pd[2] : pd[0], n1 = pd[1], n2 = hdf5_order ? pd[0] : pd[2];
+  if (!dims_ok(n0, n1, n2)) {
+    h5_field_close(hphi);
+    return set_error(SRT_ERR_INVALID_ARGUMENT, "srt_fields_load_h5: bad grid extents %lld x %lld x %lld",
+                     (long long)n0, (long long)n1, (long long)n2);
+  }
+  // without a device both files are still read (and checked) before the
+  // device error, in the reference's order
+  const bool have_device = srt_device_count() > 0;
+  bool cancelled = progress && progress(SRT_LOAD_PHI_DIMS, pd, ctx) != 0;
+  if (cancelled) {
+    h5_field_close(hphi);
+    return set_error(SRT_ERR_CANCELLED, "srt_fields_load_h5: stopped by the progress callback");
+  }
+  const int64_t plane = n0 * n1, vox = plane * n2;
+  int64_t phi_count = 1;  // every element of phi is read (the first vox are traced)
+  for (int d = 0; d < prank; ++d) phi_count *= pd[d];
+  float* hphi_data = (float*)malloc((size_t)phi_count * sizeof(float));
+  float* hb_data = (float*)malloc((size_t)(3 * vox) * sizeof(float));
+  if (!hphi_data || !hb_data) {
+    free(hphi_data);
+    free(hb_data);
+    h5_field_close(hphi);
+    return set_error(SRT_ERR_OUT_OF_MEMORY, "srt_fields_load_h5: cannot allocate host memory for the fields");
+  }
+  // ---- the reader thread: phi, then B; progress published under a mutex
+  struct Shared {
+    std::mutex m;
+    std::condition_variable cv;
+    int64_t ready[2] = {0, 0};  // floats of phi / B in their final host values
+    int stage = 0;              // 0 reading phi, 1 phi read, 2 B header read, 3 done
+    int rc = SRT_OK;
+    std::string err;
+    int64_t bd[8] = {0};
+    double read_ms[2] = {0, 0};
+    bool stop = false;  // set by this thread when it gives up: the reader stops
+  } sh;
+  auto publish = [&](int field, int64_t n) {
+    std::lock_guard<std::mutex> lk(sh.m);
+    sh.ready[field] = n;
+    sh.cv.notify_all();
+    return !sh.stop;
+  };
+  std::thread reader([&, hphi]() {
+    char buf[1024];
+    auto t0 = std::chrono::steady_clock::now();
+    int r = h5_field_read(hphi, hphi_data, phi_scale, [&](int64_t n) { return publish(0, n); });
+    h5_field_close(hphi);
+    auto fail_with = [&](int code) {
+      srt_last_error(buf, sizeof(buf));
+      std::lock_guard<std::mutex> lk(sh.m);
+      sh.rc = code;
+      sh.err = buf;
+      sh.stage = 3;
+      sh.cv.notify_all();
+    };
+    if (r != SRT_OK) return fail_with(r);
+    {
+      std::lock_guard<std::mutex> lk(sh.m);
+      sh.read_ms[0] = ms_since(t0);
+      sh.stage = 1;
+      sh.cv.notify_all();
+    }
+    H5Field* hb = nullptr;
+    int64_t bd[8] = {0};
+    int brank = 0;
+    {
+      std::lock_guard<std::mutex> lk(sh.m);
+      if (sh.stop) return;
+    }
+    r = h5_field_open(b_path, dset, true, bd, &brank, &hb);
+    if (r == SRT_OK && (bd[0] != pd[0] || bd[1] != pd[1] || bd[2] != pd[2]))
+      r = set_error(SRT_ERR_FORMAT, "B field dimensions %lld x %lld x %lld differ from the potential's",
+                    (long long)bd[0], (long long)bd[1], (long long)bd[2]);
+    if (r != SRT_OK) {
+      if (hb) h5_field_close(hb);
+      return fail_with(r);
+    }
+    {
+      std::lock_guard<std::mutex> lk(sh.m);
+      for (int i = 0; i < 3; ++i) sh.bd[i] = bd[i];
+      sh.stage = 2;
+      sh.cv.notify_all();
+    }
+    t0 = std::chrono::steady_clock::now();
+    r = h5_field_read(hb, hb_data, b_scale, [&](int64_t n) { return publish(1, n); });
+    h5_field_close(hb);
+    std::lock_guard<std::mutex> lk(sh.m);
+    sh.read_ms[1] = ms_since(t0);
+    if (r != SRT_OK) {
+      srt_last_error(buf, sizeof(buf));
+      sh.rc = r;
+      sh.err = buf;
+    }
+    sh.stage = 3;
+    sh.cv.notify_all();
+  });
+  // ---- this thread: lay out each run of planes as soon as it has been read
+  cudaStream_t s = nullptr;
+  srt_fields* f = new (std::nothrow) srt_fields();
+  float* slab = nullptr;
+  double layout_ms = 0.0, tail_ms = 0.0;
+  bool announced_b = false, announced_bdims = false, announced_upload = false;
+  rc = f ? SRT_OK : set_error(SRT_ERR_OUT_OF_MEMORY, "srt_fields_load_h5: host allocation failed");
+  if (rc == SRT_OK && have_device) rc = alloc_fields(f, n0, n1, n2, s);
+  int64_t kslab = kSlabBytes / (plane * 3 * (int64_t)sizeof(float));
+  if (kslab < 1) kslab = 1;
+  if (kslab > n2) kslab = n2;
+  if (rc == SRT_OK && have_device) {
+    cudaError_t e = pool_alloc((void**)&slab, kslab * plane * 3 * sizeof(float), s);
+    if (e != cudaSuccess) rc = cuda_error(e, "allocate slab");
+  }
+  auto announce = [&](int event, const int64_t* d) {
+    if (progress && !cancelled && progress(event, d, ctx) != 0) cancelled = true;
+  };
+  std::chrono::steady_clock::time_point t_read_end;
+  for (int field = 0; field < 2 && rc == SRT_OK; ++field) {
+    const int comps = field == 0 ? 1 : 3;
+    const float* host = field == 0 ? hphi_data : hb_data;
+    float* const phi_dst[3] = {f->phi, nullptr, nullptr};
+    for (int64_t k0 = 0; k0 < n2 && rc == SRT_OK; k0 += kslab) {
+      const int64_t k1 = k0 + kslab < n2 ? k0 + kslab : n2;
+      const int64_t need = k1 * plane * comps;
+      {
+        std::unique_lock<std::mutex> lk(sh.m);
+        while (true) {
+          // the steps the reference prints, in its order, as they happen
+          if (!announced_b && sh.stage >= 1 && sh.read_ms[0] > 0.0) {
+            announced_b = true;
+            lk.unlock();
+            announce(SRT_LOAD_B_START, pd);
+            lk.lock();
+            continue;
+          }
+          if (!announced_bdims && sh.stage >= 2 && sh.rc == SRT_OK) {
+            announced_bdims = true;
+            int64_t bd[3] = {sh.bd[0], sh.bd[1], sh.bd[2]};
+            lk.unlock();
+            announce(SRT_LOAD_B_DIMS, bd);
+            lk.lock();
+            continue;
+          }
+          if (sh.rc != SRT_OK || cancelled) break;
+          if (sh.ready[field] >= need) break;
+          sh.cv.wait(lk);
+        }
+        if (sh.rc != SRT_OK) {
+          rc = set_error(sh.rc, "%s", sh.err.c_str());
+          break;
+        }
+        if (cancelled) {
+          rc = set_error(SRT_ERR_CANCELLED, "srt_fields_load_h5: stopped by the progress callback");
+          break;
+        }
+        if (sh.stage == 3 && announced_bdims && !announced_upload) {
+          announced_upload = true;
+          t_read_end = std::chrono::steady_clock::now();
+          lk.unlock();
+          announce(SRT_LOAD_UPLOAD, sh.bd);
+          lk.lock();
+        }
+      }
+      if (cancelled) {
+        rc = set_error(SRT_ERR_CANCELLED, "srt_fields_load_h5: stopped by the progress callback");
+        break;
+      }
+      if (!have_device) continue;  // read and checked only
+      const auto tl = std::chrono::steady_clock::now();
+      cudaError_t e = cudaMemcpyAsync(slab, host + k0 * plane * comps, (k1 - k0) * plane * comps * sizeof(float),
+                                      cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = launch_pad_fields(slab, comps, field == 0 ? phi_dst : f->b, f->n, f->pn, k0, k1, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) rc = cuda_error(e, "srt_fields_load_h5: layout");
+      layout_ms += ms_since(tl);
+    }
+  }
+  if (rc != SRT_OK) {  // let the reader stop at its next progress call
+    std::lock_guard<std::mutex> lk(sh.m);
+    sh.stop = true;
+  }
+  reader.join();
+  if (rc == SRT_OK && sh.rc != SRT_OK) rc = set_error(sh.rc, "%s", sh.err.c_str());
+  if (rc == SRT_OK && !announced_upload) {
+    t_read_end = std::chrono::steady_clock::now();
+    announce(SRT_LOAD_UPLOAD, sh.bd);
+    if (cancelled) rc = set_error(SRT_ERR_CANCELLED, "srt_fields_load_h5: stopped by the progress callback");
+  }
+  if (rc == SRT_OK && !have_device) rc = set_error(SRT_ERR_NO_DEVICE, "srt_fields_load_h5: no CUDA device");
+  free(hphi_data);
+  free(hb_data);
+  if (slab) pool_free(slab, s);
+  if (rc == SRT_OK) {
+    const auto tt = std::chrono::steady_clock::now();
+    rc = build_row_pairs(f, flags & SRT_FIELDS_NO_PAIRS, s);
+    if (rc == SRT_OK) {
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) rc = cuda_error(e, "srt_fields_load_h5");
+    }
+    tail_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_read_end).count();
+    (void)tt;
+  }
+  if (rc != SRT_OK) {
+    cudaStreamSynchronize(s);
+    srt_fields_destroy(f);
+    return rc;
+  }
+  if (stats) {
+    stats->read_phi_ms = sh.read_ms[0];
+    stats->read_b_ms = sh.read_ms[1];
+    stats->layout_ms = layout_ms;
+    stats->after_read_ms = tail_ms;
+    stats->total_ms = ms_since(t_start);
+    stats->h2d_bytes = 4 * vox * (int64_t)sizeof(float);
+    for (int i = 0; i < 3; ++i) stats->n[i] = f->n[i];
+  }
+  *out = f;
+  return SRT_OK;
 }
 
 int srt_pix2ang_ring(int64_t nside, int64_t pix, double* theta, double* phi) {

@@ -79,23 +79,6 @@ bool parse_f64(const char* s, double* v) {
   return true;
 }
 
-// data[i] = float(data[i] * factor) over count values, on all host threads.
-void rescale(float* data, int64_t count, double factor) {
-  unsigned nt = std::thread::hardware_concurrency();
-  if (nt < 1) nt = 1;
-  if (count < (int64_t(1) << 20)) nt = 1;
-  std::vector<std::thread> pool;
-  const int64_t chunk = (count + nt - 1) / nt;
-  for (unsigned t = 0; t < nt; ++t) {
-    const int64_t lo = t * chunk, hi = lo + chunk < count ? lo + chunk : count;
-    if (lo >= hi) break;
-    pool.emplace_back([=] {
-      for (int64_t i = lo; i < hi; ++i) data[i] = (float)((double)data[i] * factor);
-    });
-  }
-  for (auto& th : pool) th.join();
-}
-
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -202,86 +185,63 @@ int main(int argc, char* argv[]) {
   std::cout << "n_steps: " << n_steps << std::endl;
   std::cout << "Loading potential data from HDF5 file " << pos[0] << " ..." << std::endl;
 
-  float* phi = nullptr;
-  int64_t dims[8] = {0};
-  int rank = 0;
-  if (srt_h5_read_scalar(pos[0], "/data", &phi, dims, &rank) != SRT_OK) {
-    std::cerr << last_error() << std::endl;
-    return -1;
-  }
-  if (rank < 3) {
-    std::cerr << "Expected a 3D potential dataset, got rank=" << rank << std::endl;
-    srt_free(phi);
-    return -1;
-  }
-  std::cout << "Data dimensions: " << dims[0] << " x " << dims[1] << " x " << dims[2] << std::endl;
-  if (rescale_phi) {
-    std::cout << "Rescaling potential data by factor " << phi_factor << std::endl;
-    int64_t count = 1;
-    for (int d = 0; d < rank; ++d) count *= dims[d];
-    rescale(phi, count, phi_factor);
-  }
-  const double t_phi = now_ms();
-
-  std::cout << "Loading B field data from HDF5 file " << pos[1] << " ..." << std::endl;
-  float* bxyz = nullptr;
-  int64_t bdims[3] = {0, 0, 0};
-  if (srt_h5_read_vector3(pos[1], "/data", &bxyz, bdims) != SRT_OK) {
-    std::cerr << last_error() << std::endl;
-    srt_free(phi);
-    return -1;
-  }
-  if (bdims[0] != dims[0] || bdims[1] != dims[1] || bdims[2] != dims[2]) {
-    std::cerr << "B field dimensions " << bdims[0] << " x " << bdims[1] << " x " << bdims[2]
-              << " differ from the potential's" << std::endl;
-    srt_free(phi);
-    srt_free(bxyz);
-    return -1;
-  }
-  {
-    // the reference's size warning for a large B (snapshot-raytracer.cu:159-161)
-    const double b_bytes = 3.0 * (double)bdims[0] * (double)bdims[1] * (double)bdims[2] * sizeof(float);
-    if (b_bytes > 8.0 * 1024 * 1024 * 1024)
-      std::cerr << "Warning: allocating ~" << b_bytes / (1024.0 * 1024 * 1024) << " GiB for vector field." << std::endl;
-  }
-  if (rescale_b) {
-    std::cout << "Rescaling B field data by factor " << b_factor << std::endl;
-    rescale(bxyz, 3 * bdims[0] * bdims[1] * bdims[2], b_factor);
-  }
-  const double t_b = now_ms();
-
+  // Both files are read by the library's reader thread while every finished
+  // run of planes is laid out on the device (the reference reads both files,
+  // then copies: snapshot-raytracer.cu:640, :676, :752-855); the progress
+  // callback prints the reference's lines in the reference's order.
+  // batch checks once both files are read, where the reference makes them
+  // (snapshot-raytracer.cu:708-717)
   const int64_t npix = 12 * nside * nside;
   int64_t istart = 0, count = npix;
   if (batch >= 0) {
     istart = (int64_t)batch * nside * nside;
     count = nside * nside;
-    if (istart >= npix) {
-      std::cerr << "Batch exceeds total number of pixels" << std::endl;
-      srt_free(phi);
-      srt_free(bxyz);
-      return -1;
-    }
   }
   const bool nested = base_pixel && batch >= 0;
-  if (nested && (nside & (nside - 1)) != 0) {
-    std::cerr << "--base-pixel needs a power-of-two Nside, got " << nside << std::endl;
-    srt_free(phi);
-    srt_free(bxyz);
-    return -1;
-  }
-  // grid extents, fastest first
-  const int64_t g0 = hdf5_order ? dims[2] : dims[0], g2 = hdf5_order ? dims[0] : dims[2];
-
-  std::cout << "Allocating device memory and copying data to device..." << std::endl;
+  struct Ctx {
+    const char* b_path;
+    bool rescale_phi, rescale_b;
+    double phi_factor, b_factor;
+    bool batch_past_end, bad_nested;
+    int64_t nside;
+  } ctx{pos[1], rescale_phi, rescale_b, phi_factor, b_factor, istart >= npix,
+        nested && (nside & (nside - 1)) != 0, nside};
+  auto on_progress = [](int event, const int64_t* d, void* vp) -> int {
+    Ctx* c = (Ctx*)vp;
+    if (event == SRT_LOAD_PHI_DIMS) {
+      std::cout << "Data dimensions: " << d[0] << " x " << d[1] << " x " << d[2] << std::endl;
+      if (c->rescale_phi) std::cout << "Rescaling potential data by factor " << c->phi_factor << std::endl;
+    } else if (event == SRT_LOAD_B_START) {
+      std::cout << "Loading B field data from HDF5 file " << c->b_path << " ..." << std::endl;
+    } else if (event == SRT_LOAD_B_DIMS) {
+      // the reference's size warning for a large B (snapshot-raytracer.cu:159-161)
+      const double b_bytes = 3.0 * (double)d[0] * (double)d[1] * (double)d[2] * sizeof(float);
+      if (b_bytes > 8.0 * 1024 * 1024 * 1024)
+        std::cerr << "Warning: allocating ~" << b_bytes / (1024.0 * 1024 * 1024) << " GiB for vector field."
+                  << std::endl;
+      if (c->rescale_b) std::cout << "Rescaling B field data by factor " << c->b_factor << std::endl;
+    } else if (event == SRT_LOAD_UPLOAD) {
+      if (c->batch_past_end) {
+        std::cerr << "Batch exceeds total number of pixels" << std::endl;
+        return 1;
+      }
+      if (c->bad_nested) {
+        std::cerr << "--base-pixel needs a power-of-two Nside, got " << c->nside << std::endl;
+        return 1;
+      }
+      std::cout << "Allocating device memory and copying data to device..." << std::endl;
+    }
+    return 0;
+  };
   srt_fields* fields = nullptr;
-  if (srt_fields_create(phi, bxyz, g0, dims[1], g2, 0, nullptr, &fields) != SRT_OK) {
-    std::cerr << "Failed to copy data to device: " << last_error() << std::endl;
-    srt_free(phi);
-    srt_free(bxyz);
+  srt_load_stats ls;
+  const unsigned lflags = hdf5_order ? SRT_LOAD_XYZ_HDF5 : 0u;
+  const int lrc = srt_fields_load_h5(pos[0], pos[1], "/data", lflags, rescale_phi ? phi_factor : 1.0,
+                                     rescale_b ? b_factor : 1.0, on_progress, &ctx, &fields, &ls);
+  if (lrc != SRT_OK) {
+    if (lrc != SRT_ERR_CANCELLED) std::cerr << last_error() << std::endl;  // else the callback said why
     return -1;
   }
-  srt_free(bxyz);
-  srt_free(phi);
   const double t_up = now_ms();
 
   std::cout << "Computing theta and phi angles..." << std::endl;
@@ -329,10 +289,14 @@ int main(int argc, char* argv[]) {
   const double t_end = now_ms();
   std::cout << "All done!" << std::endl;
   if (timing) {
-    printf("{\"load_phi_ms\": %.3f, \"load_b_ms\": %.3f, \"upload_ms\": %.3f, \"trace_ms\": %.3f, "
-           "\"trace_kernel_ms\": %.3f, \"write_ms\": %.3f, \"total_ms\": %.3f, \"rays\": %lld, \"ray_steps\": %lld}\n",
-           t_phi - t_start, t_b - t_phi, t_up - t_b, t_trace - t_up, st.trace_ms, t_end - t_trace, t_end - t_start,
-           (long long)st.rays, (long long)st.ray_steps);
+    // read_*: the reader thread; layout_ms: copies and layout, overlapped with
+    // the reads; after_read_ms: from the end of the reads to the fields being
+    // ready (what the upload adds to the reads)
+    printf("{\"read_phi_ms\": %.3f, \"read_b_ms\": %.3f, \"layout_ms\": %.3f, \"after_read_ms\": %.3f, "
+           "\"load_ms\": %.3f, \"trace_ms\": %.3f, \"trace_kernel_ms\": %.3f, \"write_ms\": %.3f, "
+           "\"total_ms\": %.3f, \"rays\": %lld, \"ray_steps\": %lld}\n",
+           ls.read_phi_ms, ls.read_b_ms, ls.layout_ms, ls.after_read_ms, t_up - t_start, t_trace - t_up, st.trace_ms,
+           t_end - t_trace, t_end - t_start, (long long)st.rays, (long long)st.ray_steps);
   }
   return 0;
 }

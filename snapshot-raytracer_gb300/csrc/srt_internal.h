@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
+#include <functional>
 #include <string>
 #include <nvtx3/nvToolsExt.h>
 #include "srt.h"
@@ -77,6 +78,18 @@ cudaError_t launch_pair_build(const float* src, float2* dst, const int64_t pn[3]
 cudaError_t launch_trace(int mode, const TraceArgs& a, cudaStream_t s, int64_t* kernels);
 // FP64 re-trace of the rays listed by a MIXED trace (count read on the device).
 cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels);
+
+// Progressive reads of an HDF5 field (srt_io.cpp), for srt_fields_load_h5.
+// h5_field_open reads the header and checks the dataset as
+// srt_h5_read_scalar (vector3 false) or srt_h5_read_vector3 (true) do;
+// h5_field_read fills `out` (all elements as floats, times `scale`) in order
+// along the slowest axis and calls ready(n) once the first n floats are final;
+// ready returning false stops the read (the call then returns
+// SRT_ERR_CANCELLED).
+struct H5Field;
+int h5_field_open(const char* path, const char* dset, bool vector3, int64_t dims[8], int* rank, H5Field** out);
+int h5_field_read(H5Field* h, float* out, double scale, const std::function<bool(int64_t)>& ready);
+void h5_field_close(H5Field* h);
 
 // Forgets srt_forward_noalloc's cached scratch addresses (srt_noalloc.cu).
 void noalloc_forget_scratch();

@@ -28,6 +28,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <exception>
+#include <functional>
 #include <mutex>
 #include <new>
 #include <string>
@@ -597,25 +598,58 @@ struct Reader {
     return buf;
   }
 
-  // raw bytes of the whole dataset in C order
-  std::vector<uint8_t> read_all(const Dataset& d) {
+  // bytes of the whole dataset in C order
+  static uint64_t total_bytes(const Dataset& d) {
     uint64_t nelem = 1;
     for (auto v : d.dims) nelem *= v;
     const uint64_t es = (uint64_t)d.type.size;
     if (d.dims.size() && nelem / d.dims.back() != 0 && es * nelem / es != nelem) fail(SRT_ERR_FORMAT, "size overflow");
-    const uint64_t total = nelem * es;
+    return nelem * es;
+  }
+
+  // raw bytes of the whole dataset in C order
+  std::vector<uint8_t> read_all(const Dataset& d) {
+    std::vector<uint8_t> out(total_bytes(d));
+    read_into(d, out.data(), nullptr);
+    return out;
+  }
+
+  // The same into `out` (total_bytes(d) bytes), in order along the slowest
+  // axis where the layout allows: ready(n) is called, with n growing, once
+  // the first n bytes of `out` hold their final values (contiguous data in
+  // 64 MB reads; chunked data one row of chunks along the slowest axis at a
+  // time; anything else at the end).
+  void read_into(const Dataset& d, uint8_t* out, const std::function<void(uint64_t)>& ready) {
+    const uint64_t es = (uint64_t)d.type.size;
+    const uint64_t total = total_bytes(d);
+    auto done = [&](uint64_t n) {
+      if (ready) ready(n);
+    };
     if (d.layout == 0) {
       if (d.compact.size() < total) fail(SRT_ERR_FORMAT, "compact data too short");
-      return std::vector<uint8_t>(d.compact.begin(), d.compact.begin() + total);
+      memcpy(out, d.compact.data(), total);
+      done(total);
+      return;
     }
     if (d.layout == 1) {
-      if (d.addr == kUndef) return std::vector<uint8_t>(total, 0);  // never written: fill value 0
-      return bytes(d.addr, total);
+      if (d.addr == kUndef) {  // never written: fill value 0
+        memset(out, 0, total);
+        done(total);
+        return;
+      }
+      const uint64_t block = uint64_t(64) << 20;
+      for (uint64_t o = 0; o < total; o += block) {
+        const uint64_t n = std::min(block, total - o);
+        if (!F.read_at(base + d.addr + o, out + o, n)) fail(SRT_ERR_FORMAT, "read past end of file");
+        done(o + n);
+      }
+      if (total == 0) done(0);
+      return;
     }
     // chunked
     const size_t rank = d.dims.size();
     if (d.chunk.size() != rank) fail(SRT_ERR_FORMAT, "chunk rank mismatch");
-    std::vector<uint8_t> out(total, 0);
+    memset(out, 0, total);
     uint64_t cbytes = es;
     for (auto c : d.chunk) cbytes *= c;
     auto place = [&](const std::vector<uint8_t>& cb, const std::vector<uint64_t>& origin) {
@@ -646,7 +680,8 @@ struct Reader {
       std::vector<uint8_t> cb = unfilter(d, bytes(d.addr, sz), 0, cbytes);
       if (cb.size() < cbytes) cb.resize(cbytes, 0);
       place(cb, std::vector<uint64_t>(rank, 0));
-      return out;
+      done(total);
+      return;
     }
     if (d.layout_ver == 4 && d.chunk_index == 2) {  // implicit: chunks stored in order, unfiltered
       std::vector<uint64_t> nch(rank);
@@ -664,7 +699,8 @@ struct Reader {
         }
         place(bytes(d.addr + c * cbytes, cbytes), origin);
       }
-      return out;
+      done(total);
+      return;
     }
     // v1 B-tree of chunks (node type 1): collect the leaf chunks, then read
     // and unfilter them on all host threads (each chunk lands in its own
@@ -705,15 +741,25 @@ struct Reader {
         leaves.push_back(Leaf{child, csz, mask, origin});
       }
     }
-    unsigned nt = std::thread::hardware_concurrency();
-    if (nt < 1) nt = 1;
-    nt = (unsigned)std::min<size_t>(nt, leaves.size() / 4 + 1);
-    std::atomic<size_t> next{0};
+    // rows of chunks along the slowest axis, in order, so that the output
+    // fills from the front (each row read and unfiltered on all threads)
+    std::stable_sort(leaves.begin(), leaves.end(),
+                     [](const Leaf& a, const Leaf& b) { return a.origin[0] < b.origin[0]; });
+    uint64_t row_bytes = es;  // bytes of one index of the slowest axis
+    for (size_t k = 1; k < rank; ++k) row_bytes *= d.dims[k];
+    unsigned nt_all = std::thread::hardware_concurrency();
+    if (nt_all < 1) nt_all = 1;
     std::mutex err_mutex;
     bool failed = false;
     H5Error first{0, ""};
+    size_t row_lo = 0;
+    while (row_lo < leaves.size() && !failed) {
+    size_t row_hi = row_lo;
+    while (row_hi < leaves.size() && leaves[row_hi].origin[0] == leaves[row_lo].origin[0]) ++row_hi;
+    const unsigned nt = (unsigned)std::min<size_t>(nt_all, (row_hi - row_lo) / 4 + 1);
+    std::atomic<size_t> next{row_lo};
     auto work = [&]() {
-      for (size_t i = next++; i < leaves.size(); i = next++) {
+      for (size_t i = next++; i < row_hi; i = next++) {
         try {
           const Leaf& L = leaves[i];
           std::vector<uint8_t> raw(L.size);
@@ -725,18 +771,18 @@ struct Reader {
           std::lock_guard<std::mutex> lock(err_mutex);
           if (!failed) first = e;
           failed = true;
-          next = leaves.size();
+          next = row_hi;
         } catch (const std::bad_alloc&) {
           // an exception that left a worker thread would end the process
           std::lock_guard<std::mutex> lock(err_mutex);
           if (!failed) first = H5Error{SRT_ERR_OUT_OF_MEMORY, "out of host memory while reading chunks"};
           failed = true;
-          next = leaves.size();
+          next = row_hi;
         } catch (const std::exception& e) {
           std::lock_guard<std::mutex> lock(err_mutex);
           if (!failed) first = H5Error{SRT_ERR_FORMAT, std::string("chunk read failed: ") + e.what()};
           failed = true;
-          next = leaves.size();
+          next = row_hi;
         }
       }
     };
@@ -747,8 +793,15 @@ struct Reader {
       for (unsigned t = 0; t < nt; ++t) pool.emplace_back(work);
       for (auto& th : pool) th.join();
     }
+    if (!failed) {
+      const uint64_t rows_done = std::min<uint64_t>(d.dims[0], leaves[row_lo].origin[0] + d.chunk[0]);
+      // the next row of chunks starts at or after rows_done (chunks are aligned)
+      done(row_hi < leaves.size() ? std::min<uint64_t>(total, rows_done * row_bytes) : total);
+    }
+    row_lo = row_hi;
+    }
     if (failed) throw first;
-    return out;
+    if (leaves.empty()) done(total);
   }
 };
 
@@ -807,6 +860,97 @@ std::vector<uint8_t> dtype_msg(int vector3) {
 }  // namespace
 
 using srt::set_error;
+
+// ------------------------------------------------ progressive field reads
+
+namespace srt {
+
+struct H5Field {
+  Reader R;
+  Dataset d;
+  std::string path;
+  bool vector3 = false;
+};
+
+int h5_field_open(const char* path, const char* dset, bool vector3, int64_t dims[8], int* rank, H5Field** out) {
+  *out = nullptr;
+  H5Field* h = new (std::nothrow) H5Field();
+  if (!h) return set_error(SRT_ERR_OUT_OF_MEMORY, "%s: out of host memory", path);
+  try {
+    h->path = path;
+    h->vector3 = vector3;
+    if (!h->R.F.open(path)) {
+      delete h;
+      return set_error(SRT_ERR_IO, "Failed to open HDF5 file: %s", path);
+    }
+    h->R.superblock();
+    h->d = h->R.dataset(h->R.resolve(dset));
+    const Dataset& d = h->d;
+    int rc = SRT_OK;
+    if (!vector3) {
+      if (d.dims.size() > 8) rc = set_error(SRT_ERR_UNSUPPORTED, "%s: rank %zu > 8", path, d.dims.size());
+      else if (d.type.cls == 10)
+        rc = set_error(SRT_ERR_FORMAT, "%s: %s has an array element type, expected scalars", path, dset);
+    } else {  // the reference's checks, snapshot-raytracer.cu:113-143
+      if (d.dims.size() != 3) rc = set_error(SRT_ERR_FORMAT, "Expected 3D dataspace, got rank=%zu", d.dims.size());
+      else if (d.type.cls != 10)
+        rc = set_error(SRT_ERR_FORMAT, "Dataset is not an array type (expected array[3] of float).");
+      else if (d.type.adims.size() != 1 || d.type.adims[0] != 3)
+        rc = set_error(SRT_ERR_FORMAT, "Expected per-voxel array length 3, got length=%llu",
+                       (unsigned long long)(d.type.adims.empty() ? 0 : d.type.adims[0]));
+    }
+    if (rc != SRT_OK) {
+      delete h;
+      return rc;
+    }
+    *rank = (int)d.dims.size();
+    for (size_t i = 0; i < d.dims.size() && i < 8; ++i) dims[i] = (int64_t)d.dims[i];
+    *out = h;
+    return SRT_OK;
+  } catch (const H5Error& e) {
+    delete h;
+    return h5_status(e, path);
+  } catch (const std::bad_alloc&) {
+    delete h;
+    return set_error(SRT_ERR_OUT_OF_MEMORY, "%s: out of host memory", path);
+  }
+}
+
+int h5_field_read(H5Field* h, float* out, double scale, const std::function<bool(int64_t)>& ready) {
+  const Dataset& d = h->d;
+  const bool vec = h->vector3;
+  const int es = vec ? d.type.base_size : d.type.size;
+  const int cls = vec ? d.type.base_cls : d.type.cls;
+  const bool big = vec ? d.type.base_big : d.type.big;
+  const bool sign = vec ? d.type.base_sign : d.type.sign;
+  const bool native = cls == 1 && es == 4 && !big;
+  try {
+    uint64_t n = vec ? 3 : 1;  // floats
+    for (auto v : d.dims) n *= v;
+    std::vector<uint8_t> raw;
+    if (!native) raw.resize((size_t)(n * es));
+    uint8_t* dst = native ? (uint8_t*)out : raw.data();
+    uint64_t conv = 0;  // floats converted (and scaled) so far
+    h->R.read_into(d, dst, [&](uint64_t bytes) {
+      const uint64_t upto = bytes / (uint64_t)es;
+      if (!native)
+        for (uint64_t i = conv; i < upto; ++i) out[i] = (float)load_num(&raw[i * es], cls, es, big, sign);
+      if (scale != 1.0)
+        for (uint64_t i = conv; i < upto; ++i) out[i] = (float)((double)out[i] * scale);
+      conv = upto;
+      if (ready && !ready((int64_t)upto)) fail(SRT_ERR_CANCELLED, "read stopped");
+    });
+    return SRT_OK;
+  } catch (const H5Error& e) {
+    return h5_status(e, h->path.c_str());
+  } catch (const std::bad_alloc&) {
+    return set_error(SRT_ERR_OUT_OF_MEMORY, "%s: out of host memory", h->path.c_str());
+  }
+}
+
+void h5_field_close(H5Field* h) { delete h; }
+
+}  // namespace srt
 
 extern "C" {
 

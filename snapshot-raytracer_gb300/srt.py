@@ -31,7 +31,7 @@ SRT_NESTED_RANGE = 128
 SRT_FIELDS_STAGED = 256
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "I/O error",
-          -5: "format error", -6: "no CUDA device", -7: "unsupported", -8: "overflow"}
+          -5: "format error", -6: "no CUDA device", -7: "unsupported", -8: "overflow", -9: "cancelled"}
 
 
 class SrtError(RuntimeError):
@@ -48,6 +48,19 @@ class Stats(ctypes.Structure):
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
+
+class LoadStats(ctypes.Structure):
+    _fields_ = [("read_phi_ms", ctypes.c_double), ("read_b_ms", ctypes.c_double), ("layout_ms", ctypes.c_double),
+                ("after_read_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_int64),
+                ("n", ctypes.c_int64 * 3)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "n"}
+        d["n"] = tuple(self.n)
+        return d
+
+
+SRT_LOAD_XYZ_HDF5 = 512
 
 _lib = None
 _P = ctypes.c_void_p
@@ -95,6 +108,9 @@ def lib():
                                                  ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_int)]),
             "srt_free": (None, [_P]),
             "srt_release_cached_memory": (ctypes.c_int, []),
+            "srt_fields_load_h5": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint,
+                                                  ctypes.c_double, ctypes.c_double, _P, _P, ctypes.POINTER(_P),
+                                                  ctypes.POINTER(LoadStats)]),
             "srt_debug_fail_alloc": (ctypes.c_int, [_I64]),
         }
         for name, (res, args) in sig.items():
@@ -190,6 +206,21 @@ class Fields:
         _check(lib().srt_fields_create(p_phi, p_b, self.n[0], self.n[1], self.n[2], flags, _stream_ptr(stream),
                                        ctypes.byref(h)))
         self._h = h
+
+    @classmethod
+    def load_h5(cls, phi_path, b_path, dset="/data", xyz_order="reference", phi_scale=1.0, b_scale=1.0, pairs=True):
+        """Fields read from the reference's two HDF5 files and laid out on the
+        device while they are read (srt_fields_load_h5). Returns (Fields,
+        LoadStats dict)."""
+        self = cls.__new__(cls)
+        h = _P()
+        st = LoadStats()
+        flags = (SRT_LOAD_XYZ_HDF5 if xyz_order == "hdf5" else 0) | (0 if pairs else SRT_FIELDS_NO_PAIRS)
+        _check(lib().srt_fields_load_h5(phi_path.encode(), b_path.encode(), dset.encode(), flags, phi_scale, b_scale,
+                                        None, None, ctypes.byref(h), ctypes.byref(st)))
+        self._h = h
+        self.n = tuple(st.n)
+        return self, st.as_dict()
 
     @property
     def handle(self):

@@ -166,3 +166,53 @@ def test_cli_chunked_filtered_inputs_equal_contiguous(srt, tmp_path, filters):
         want = srt.fits_read_map(str(plain / ("%s_batch2.fits" % name)))[0]
         got = srt.fits_read_map(str(chunked / ("%s_batch2.fits" % name)))[0]
         assert np.any(want) and np.array_equal(got.view(np.uint32), want.view(np.uint32)), name
+
+
+@pytest.mark.parametrize("layout", ["contiguous", "chunked", "hdf5-order"])
+def test_fields_load_h5_equals_host_arrays(srt, tmp_path, layout):
+    """srt_fields_load_h5 reads the two files on a reader thread while every
+    finished run of planes is copied and laid out on the device: the handle
+    traces exactly as one made by srt_fields_create from the same arrays
+    (contiguous and chunked/deflated files, rescaled values, the HDF5 axis
+    order of a non-cubic grid), and its statistics account for the bytes."""
+    import ctypes
+
+    import h5_variants
+
+    shape = (20, 24, 28) if layout == "hdf5-order" else (24, 24, 24)
+    phi, b = srt_fields.gaussian_fields_np(shape, seed=14)  # numpy shape (n2, n1, n0)
+    pp, pb = str(tmp_path / "phi.h5"), str(tmp_path / "B.h5")
+    if layout == "chunked":
+        try:
+            ctypes.CDLL("libz.so.1")
+            filters = ("shuffle", "deflate")
+        except OSError:
+            filters = ()
+        h5_variants.write_v2_chunked(pp, phi, chunk=(5, 7, 6), filters=filters, fanout=3)
+        h5_variants.write_v2_chunked(pb, b, chunk=(4, 6, 9), filters=filters, array3=True)
+    else:
+        srt.h5_write(pp, phi)
+        srt.h5_write(pb, b, vector3=True)
+    nside, steps = 4, 12
+    f, st = srt.Fields.load_h5(pp, pb, xyz_order="hdf5" if layout == "hdf5-order" else "reference",
+                               phi_scale=2.0, b_scale=0.5)
+    with f:
+        got, _ = f.forward(nside, steps, precision="fp64")
+    phi2 = (phi.astype(np.float64) * 2.0).astype(np.float32)
+    b2 = (b.astype(np.float64) * 0.5).astype(np.float32)
+    if layout == "hdf5-order":
+        with srt.Fields(phi2, b2) as g:  # (n2, n1, n0) = the file's shape, x fastest
+            want, _ = g.forward(nside, steps, precision="fp64")
+        assert st["n"] == (shape[0], shape[1], shape[2])
+    else:
+        with srt.Fields(phi2, b2) as g:
+            want, _ = g.forward(nside, steps, precision="fp64")
+        assert st["n"] == (24, 24, 24)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert st["h2d_bytes"] == 16 * phi.size and st["total_ms"] > 0 and st["read_phi_ms"] > 0
+    # a B file whose extents differ from phi's is refused with the CLI's message
+    q = str(tmp_path / "B_small.h5")
+    srt.h5_write(q, np.zeros((4, 4, 4, 3), np.float32), vector3=True)
+    with pytest.raises(srt.SrtError) as ei:
+        srt.Fields.load_h5(pp, q)
+    assert "differ from the potential's" in str(ei.value)

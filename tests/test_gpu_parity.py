@@ -329,3 +329,36 @@ def test_pinned_host_inputs_read_in_place_equal_staged(srt, orc, extents):
         assert np.array_equal(g.view(np.uint32), got[0].view(np.uint32))
     for m, (rms, mx) in enumerate(map_errors(got[0], want)):
         assert rms <= 1e-9 and mx <= 1e-8, (m, rms, mx)
+
+
+def test_async_staged_upload_overlapping_a_trace(srt):
+    """The pipelined use: fields created with SRT_ASYNC on one stream (host
+    input through one staging buffer, no host synchronisation) while another
+    handle traces on a second stream; after an event the new handle traces.
+    The maps equal those of a synchronous create, bit for bit."""
+    torch = pytest.importorskip("torch")
+    import srt_fields
+
+    phi, b = srt_fields.gaussian_fields_np(40, seed=23)
+    pphi = torch.empty(phi.shape, dtype=torch.float32, pin_memory=True)
+    pb = torch.empty(b.shape, dtype=torch.float32, pin_memory=True)
+    pphi.numpy()[...] = phi
+    pb.numpy()[...] = b
+    nside, steps = 8, 30
+    with srt.Fields(phi, b) as f:
+        want, _ = f.forward(nside, steps, precision="mixed")
+    s_up = torch.cuda.Stream(priority=-1)
+    s_tr = torch.cuda.Stream()
+    with srt.Fields(pphi.numpy(), pb.numpy()) as busy:
+        out_busy = torch.empty((6, 12 * nside * nside), dtype=torch.float32, device="cuda")
+        busy.forward(nside, steps, precision="mixed", out=out_busy, stream=s_tr, async_=True)
+        nxt = srt.Fields(pphi.numpy(), pb.numpy(), stream=s_up, async_=True, staged=True)
+        ev = torch.cuda.Event()
+        ev.record(s_up)
+        s_tr.wait_event(ev)
+        got = np.zeros_like(want)
+        nxt.forward(nside, steps, precision="mixed", out=got, stream=s_tr)
+        nxt.close()
+        torch.cuda.synchronize()
+        assert np.array_equal(out_busy.cpu().numpy().view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
