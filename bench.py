@@ -525,8 +525,9 @@ def run_ours(args):
               ("f64" if args.precision == "fp64" else "f32/f16"), "data": "synthetic", "config": cfg,
               "gpu_launches": kernels,
               "refined_rays_per_step": int(np.max(refined)) if refined else 0}
-    # DRAM bytes of one trace launch, from an ncu capture of this workload
-    # (profiles/trace_traffic.json); null for workloads that were not captured
+    # DRAM bytes of one trace launch: an ncu capture of a smaller case of the
+    # same kernel scaled to this workload (profiles/trace_traffic.json); null
+    # for workloads it does not cover
     traffic = None
     prof = os.path.join(ROOT, "profiles", "trace_traffic.json")
     if os.path.isfile(prof):
@@ -581,8 +582,10 @@ def run_ours(args):
         # high-priority stream while step i traces; every step still copies
         # its 17 GB in and its maps out inside the timed region, and the first
         # upload is not hidden
+        # two non-default streams: work on the legacy default stream would wait
+        # for the upload stream's work (and the upload for it)
         s_up = torch.cuda.Stream(device=dev, priority=-1)
-        s_tr = torch.cuda.current_stream(dev)
+        s_tr = torch.cuda.Stream(device=dev)
         K = args.e2e_steps + 1
         barrier(world)
         torch.cuda.synchronize()

@@ -50,6 +50,9 @@ def _nvcc_obj(src, verbose):
     # and the FP64 form is unaffected.
     cmd = [NVCC, *GENCODE, "-lineinfo", "-O3", "--use_fast_math", "-std=c++17", "-Xcompiler", "-fPIC",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-c", src, "-o", obj]
+    # extra nvcc flags, e.g. -DSRT_MIXED_MIN_BLOCKS=3 to compile the MIXED trace
+    # for three resident blocks per SM
+    cmd[1:1] = os.environ.get("SRT_NVCC_FLAGS", "").split()
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     _run(cmd, verbose)

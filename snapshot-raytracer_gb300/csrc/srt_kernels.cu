@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(128, (MODE == kMIXED || MODE == kMIXED_PAIR) ?
 // take the FP64 path.
 constexpr int64_t kRefineBlocksPerSM = 32;
 constexpr int64_t kRefineWarpsPerSubpartition = 2;
+constexpr int64_t kRefineWideWarpsPerSubpartition = 4;
 
 __device__ __forceinline__ void shfl_tri(Tri<double>& d, const Tri<double>& s, int src, unsigned mask) {
   d.v = __shfl_sync(mask, s.v, src);
@@ -275,22 +276,42 @@ __device__ __forceinline__ void step_dd_group(const FieldPtrs& F, const Geom& G,
   for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
 }
 
-// Which re-trace a list gets: up to dd_min rays the bit-exact FP64 four-lane
-// groups (one warp per sub-partition at most: latency-bound, and FP64 is
-// then the shorter), longer lists double-float four-lane groups (~1.4x
-// shorter than FP64 one-lane warps at ~19k rays, maps within one float ulp of
-// the FP64 ones). The environment variable SRT_REFINE_DD_MIN overrides dd_min
-// (tests use it to reach the double-float path on small skies).
-// MODE 4: FP64, four lanes per ray (lists up to SRT_REFINE_DD_MIN rays);
-// MODE 1: double-float, one lane per ray (longer lists).
+// step_dd_group with one lane doing the whole ray (rhs_dd: all four
+// interpolations and the right-hand side once).
+__device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, dd* y) {
+  dd acc[19], k[19], ys[19];
+#pragma unroll 1
+  for (int st = 0; st < 4; ++st) {
+    const float c = (st == 3) ? 1.f : 0.5f;
+    for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
+    rhs_dd(ys, k, F, G);
+    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
+  }
+  const dd sixth = dd(1.0 / 6.0);
+  for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
+}
+
+// Which re-trace a list of n rays gets:
+//   MODE 4 (n <= dd_min): the bit-exact FP64 four-lane groups (one warp per
+//     sub-partition at most: latency-bound, and FP64 is then the shorter);
+//   MODE 1 (dd_min < n <= wide_min): double-float four-lane groups (~1.4x
+//     shorter than FP64 one-lane warps at ~19k rays; maps within one float ulp
+//     of the FP64 ones);
+//   MODE 2 (n > wide_min): double-float, one lane per ray: once the list fills
+//     every sub-partition with several warps the launch is bound by the total
+//     work, which the four-lane groups raise by repeating the right-hand side
+//     on each lane (~48k against ~28k FP32 instructions per ray and stage).
+// The environment variables SRT_REFINE_DD_MIN and SRT_REFINE_WIDE_MIN override
+// dd_min and wide_min (tests use them to reach every path on small skies).
 template <int MODE>
-__global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t dd_min) {
-  constexpr int LANES = 4;
+__global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t dd_min, int64_t wide_min) {
+  constexpr int LANES = MODE == 2 ? 1 : 4;
   constexpr int kRays = 32 / LANES;  // rays per warp
   const int lane = threadIdx.x;
   const unsigned long long count = *A.refine_count;
   const int64_t n = min((int64_t)count, A.pix_count);
-  if ((MODE == 4) != (n <= dd_min)) return;
+  const int mode = n <= dd_min ? 4 : (n <= wide_min ? 1 : 2);
+  if (mode != MODE) return;
 #pragma unroll 1
   for (int64_t k0 = (int64_t)blockIdx.x * kRays; k0 < n; k0 += (int64_t)gridDim.x * kRays) {
     const int64_t k = k0 + lane / LANES;
@@ -308,6 +329,12 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t d
 #pragma unroll 1
       for (int step = 0; step < A.n_steps; ++step) step_fp64_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
       extract_std(d, A.G, y, out);
+    } else if (MODE == 2) {
+      dd y[19];
+      init_dd(d, A.G, y);
+#pragma unroll 1
+      for (int step = 0; step < A.n_steps; ++step) step_dd1(A.F, A.G, y);
+      extract_dd(d, A.G, y, out);
     } else {
       dd y[19];
       init_dd(d, A.G, y);
@@ -331,11 +358,16 @@ cudaError_t launch_refine(const TraceArgs& a, cudaStream_t s, int64_t* kernels) 
   if (e != cudaSuccess) return e;
   int64_t dd_min = kRefineWarpsPerSubpartition * 4 * (int64_t)sms * 8;
   if (const char* v = getenv("SRT_REFINE_DD_MIN")) dd_min = strtoll(v, nullptr, 10);
+  // one-lane rays from four warps of 32 per sub-partition on
+  int64_t wide_min = kRefineWideWarpsPerSubpartition * 4 * (int64_t)sms * 32;
+  if (const char* v = getenv("SRT_REFINE_WIDE_MIN")) wide_min = strtoll(v, nullptr, 10);
   const int64_t blocks = std::min((a.pix_count + 7) / 8, kRefineBlocksPerSM * (int64_t)sms);
   if (blocks < 1) return cudaSuccess;
-  refine_kernel<4><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min);
-  refine_kernel<1><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min);
-  if (kernels) *kernels += 2;
+  const int64_t blocks1 = std::min((a.pix_count + 31) / 32, kRefineBlocksPerSM * (int64_t)sms);
+  refine_kernel<4><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min, wide_min);
+  refine_kernel<1><<<(unsigned)blocks, 32, 0, s>>>(a, dd_min, wide_min);
+  refine_kernel<2><<<(unsigned)blocks1, 32, 0, s>>>(a, dd_min, wide_min);
+  if (kernels) *kernels += 3;
   return cudaGetLastError();
 }
 

@@ -220,18 +220,23 @@ def test_nested_range_matches_ring(srt, precision):
             f.forward(6, steps, 0, 36, precision=precision, nested=True)
 
 
-def test_mixed_refine_double_float_path(srt, monkeypatch):
-    """Long re-trace lists run in double-float arithmetic (forced here with
-    SRT_REFINE_DD_MIN=0 on a small sky): the re-traced rays agree with the
-    FP64 form to a float ulp or two, everything else is untouched."""
+@pytest.mark.parametrize("lanes", [4, 1])
+def test_mixed_refine_double_float_path(srt, monkeypatch, lanes):
+    """Long re-trace lists run in double-float arithmetic, four lanes per ray
+    (forced here with SRT_REFINE_DD_MIN=0 on a small sky) or, for the longest
+    lists, one lane per ray (SRT_REFINE_WIDE_MIN=0): the re-traced rays agree
+    with the FP64 form to a float ulp or two, everything else is untouched."""
     phi, b = srt_fields.gaussian_fields_np(128, seed=13)
     nside, steps = 32, 128
     with srt.Fields(phi, b) as f:
         m64, _ = f.forward(nside, steps, precision="fp64")
         mn, _ = f.forward(nside, steps, precision="mixed", refine=False)
         monkeypatch.setenv("SRT_REFINE_DD_MIN", "0")
+        if lanes == 1:
+            monkeypatch.setenv("SRT_REFINE_WIDE_MIN", "0")
         mr, st = f.forward(nside, steps, precision="mixed")
         monkeypatch.delenv("SRT_REFINE_DD_MIN")
+        monkeypatch.delenv("SRT_REFINE_WIDE_MIN", raising=False)
     assert st.refined_rays > 0
     changed = np.any(mr.view(np.uint32) != mn.view(np.uint32), axis=0)
     assert changed.sum() <= st.refined_rays
