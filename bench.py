@@ -476,13 +476,16 @@ def run_ours(args):
            "grid": n, "nside": nside, "rays": npix, "n_steps": S, "precision": args.precision,
            "fields": "gaussian P(k)~k^-3, phi rms 1e-5, B rms 1e-7, seed %d" % (args.seed + rank),
            "l2": "inputs larger than L2 (%.1f GB of fields vs 0.13 GB L2)" % (16 * n ** 3 / 1e9),
-           "parallelism": "replicas x%d (pixel-parallel, no collective)" % world,
-           "field_layout": "halo-padded planes" + (" + row-pair copies" if args.pairs else "")}
+           "parallelism": "replicas x%d (pixel-parallel, no collective)" % world}
 
     phi_d, b_d = srt_fields.gaussian_fields_torch(n, seed=args.seed + rank, device=dev)
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
     fields = srt.Fields(phi_d, b_d, stream=stream, pairs=args.pairs)
+    # the row-pair copies are built only when they fit (not at 2048^3)
+    with_pairs = fields.nbytes > 16 * (n + 3) ** 3
+    cfg["field_layout"] = "halo-padded planes" + (" + row-pair copies" if with_pairs else
+                                                  " (packed passes form their pairs from the single layout)")
     if args.e2e_steps <= 0:  # the laid-out copy is all the trace needs (2048^3: 137 GB freed)
         torch.cuda.synchronize()
         del phi_d, b_d
