@@ -255,10 +255,16 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
   for (int j = 0; j < 19; ++j) lam[(int64_t)j * A.count + slot] = s_lam[j][t];
 }
 
+// Resident blocks of 128 threads per SM the sweep is compiled for (register
+// budget 65536 / (128 * blocks)).
+#ifndef SRT_SWEEP_MIN_BLOCKS
+#define SRT_SWEEP_MIN_BLOCKS 2
+#endif
+
 // BGRAD: the B gradient is wanted (else the B passes are compiled without a
 // scatter).
 template <typename Acc, bool PAIR, bool BGRAD>
-__global__ void __launch_bounds__(128, 2) sweep_kernel_mixed(const AdjArgs A, int sgi, float* lam, const Acc a0,
+__global__ void __launch_bounds__(128, SRT_SWEEP_MIN_BLOCKS) sweep_kernel_mixed(const AdjArgs A, int sgi, float* lam, const Acc a0,
                                                            const Acc a1, const Acc a2, const Acc a3) {
   __shared__ float s_lam[19][128];
   __shared__ float s_tot[19][128];
