@@ -190,12 +190,58 @@ __device__ __forceinline__ void shfl_tri(Tri<double>& d, const Tri<double>& s, i
   for (int i = 0; i < 6; ++i) d.h[i] = __shfl_sync(mask, s.h[i], src);
 }
 
-// rhs_std<kFP64> with the four interpolations spread over a lane group
-// (field = lane & 3, group = the group's first lane, mask = live lanes).
+// A lane-group value of the state type (FP64 or double-float) from lane src.
+__device__ __forceinline__ double shfl_r(double v, int src, unsigned mask) { return __shfl_sync(mask, v, src); }
+__device__ __forceinline__ dd shfl_r(const dd& v, int src, unsigned mask) {
+  return dd(__shfl_sync(mask, v.hi, src), __shfl_sync(mask, v.lo, src));
+}
+
+// rhs_frame with its three normalisations (a square root and three divisions
+// each) shared out over a ray's lane group: lane f normalises vector f (n, e1,
+// e2; the phi lane repeats n) with the same operations, and the group
+// exchanges the results. gmask: the group's four lanes, which always run
+// together (they hold the same state).
+template <typename R>
+__device__ __forceinline__ void rhs_frame_group(const R* y, R* n, R* a, R* b, int field, int group,
+                                                unsigned gmask) {
+  const int v = field < 3 ? field : 0;
+  const R c0 = v == 0 ? y[3] : (v == 1 ? y[6] : y[9]);
+  const R c1 = v == 0 ? y[4] : (v == 1 ? y[7] : y[10]);
+  const R c2 = v == 0 ? y[5] : (v == 1 ? y[8] : y[11]);
+  const R r = sqrt_r(c0 * c0 + c1 * c1 + c2 * c2);
+  const R u[3] = {c0 / r, c1 / r, c2 / r};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    n[i] = shfl_r(u[i], group, gmask);
+    a[i] = shfl_r(u[i], group + 1, gmask);
+    b[i] = shfl_r(u[i], group + 2, gmask);
+  }
+}
+
+// The dA > 1/2 branch's four divisions shared out the same way: lane j forms
+// quotient j (every lane of a group takes the branch or none does).
+template <typename R>
+struct GroupDiv {
+  int field, group;
+  unsigned gmask;
+  __device__ void operator()(const R* num, const R* den, R* quo) const {
+    const R nj = field == 0 ? num[0] : (field == 1 ? num[1] : (field == 2 ? num[2] : num[3]));
+    const R dj = field == 0 ? den[0] : (field == 1 ? den[1] : (field == 2 ? den[2] : den[3]));
+    const R mine = nj / dj;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) quo[j] = shfl_r(mine, group + j, gmask);
+  }
+};
+
+// rhs_std<kFP64> with the four interpolations, the normalisations and the
+// branch's divisions spread over a lane group (field = lane & 3, group = the
+// group's first lane, mask = live lanes); every value is formed by the
+// operations rhs_std<kFP64> uses, so the results are the same bits.
 __device__ __forceinline__ void rhs_fp64_group(const double* y, double* dy, const FieldPtrs& F, const Geom& G,
                                                int field, int group, unsigned mask) {
+  const unsigned gmask = 0xfu << group;
   double n[3], a[3], b[3];
-  rhs_frame<double>(y, n, a, b);
+  rhs_frame_group<double>(y, n, a, b, field, group, gmask);
   Tri<double> own;
   {
     const float* src = (field == 3) ? F.phi : ((field == 0) ? F.b[0] : ((field == 1) ? F.b[1] : F.b[2]));
@@ -211,7 +257,7 @@ __device__ __forceinline__ void rhs_fp64_group(const double* y, double* dy, cons
     B.add(c, r, n, a, b);
   }
   shfl_tri(r, own, group + 3, mask);
-  rhs_finish<double, double>(y, n, a, b, B, r, dy);
+  rhs_finish<double, double>(y, n, a, b, B, r, dy, GroupDiv<double>{field, group, gmask});
 }
 
 // step_std<kFP64> on rhs_fp64_group.
@@ -241,8 +287,9 @@ __device__ __forceinline__ void shfl_tri_dd(Tri<dd>& d, const Tri<dd>& s, int sr
 
 __device__ __forceinline__ void rhs_dd_group(const dd* y, dd* dy, const FieldPtrs& F, const Geom& G, int field,
                                              int group, unsigned mask) {
+  const unsigned gmask = 0xfu << group;
   dd n[3], a[3], b[3];
-  rhs_frame<dd>(y, n, a, b);
+  rhs_frame_group<dd>(y, n, a, b, field, group, gmask);
   Tri<dd> own;
   {
     const float* src = (field == 3) ? F.phi : ((field == 0) ? F.b[0] : ((field == 1) ? F.b[1] : F.b[2]));
@@ -259,7 +306,7 @@ __device__ __forceinline__ void rhs_dd_group(const dd* y, dd* dy, const FieldPtr
     B.add(c, r, n, a, b);
   }
   shfl_tri_dd(r, own, group + 3, mask);
-  rhs_finish<dd, dd>(y, n, a, b, B, r, dy);
+  rhs_finish<dd, dd>(y, n, a, b, B, r, dy, GroupDiv<dd>{field, group, gmask});
 }
 
 __device__ __forceinline__ void step_dd_group(const FieldPtrs& F, const Geom& G, dd* y, int field, int group,

@@ -408,11 +408,20 @@ struct BSums {
   }
 };
 
+// The four quotients of the dA > 1/2 branch, each divided where it is formed
+// (the re-trace's lane groups share them out instead: GroupDiv).
+struct LocalDiv {
+  template <typename R>
+  SRT_HD void operator()(const R* num, const R* den, R* quo) const {
+    for (int j = 0; j < 4; ++j) quo[j] = num[j] / den[j];
+  }
+};
+
 // The right-hand side from the frame, the B sums and phi's interpolation p
 // (snapshot-raytracer.cu:462-509).
-template <typename IT, typename R = double>
+template <typename IT, typename R = double, typename Div = LocalDiv>
 SRT_HD void rhs_finish(const R* y, const R* n, const R* a, const R* b, const BSums<IT, R>& B, const Tri<IT>& p,
-                       R* dy) {
+                       R* dy, const Div& div = Div()) {
   const R dA = y[12], dAp = y[13], s1 = y[14], s2 = y[15], el1 = y[16], el2 = y[17];
   const R phi1 = 1.0 + 2.0 * p.v;
   for (int i = 0; i < 3; ++i) dy[i] = -n[i] * phi1 - B.val[i];
@@ -451,10 +460,14 @@ SRT_HD void rhs_finish(const R* y, const R* n, const R* a, const R* b, const BSu
   if (dA > 0.5) {
     const R dA2 = dA * dA;
     const R q = sqrt_r(4.0 + el1 * el1 + el2 * el2);
-    dy[13] += (s1 * s1 + s2 * s2) / (dA2 * dA);
-    dy[16] = -2.0 * s1 * q / dA2;
-    dy[17] = -2.0 * s2 * q / dA2;
-    dy[18] = -(s1 * el2 - s2 * el1) / (dA2 * (2.0 + q));
+    const R num[4] = {s1 * s1 + s2 * s2, -2.0 * s1 * q, -2.0 * s2 * q, -(s1 * el2 - s2 * el1)};
+    const R den[4] = {dA2 * dA, dA2, dA2, dA2 * (2.0 + q)};
+    R quo[4];
+    div(num, den, quo);
+    dy[13] += quo[0];
+    dy[16] = quo[1];
+    dy[17] = quo[2];
+    dy[18] = quo[3];
   } else {
     dy[16] = 0.0;
     dy[17] = 0.0;
