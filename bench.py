@@ -592,10 +592,18 @@ def run_ours(args):
         K = args.e2e_steps + 1
 
         call_ms = []  # host time of each asynchronous create call (it should return at once)
+        marks = []    # CUDA events: (upload start, upload end) on s_up, (trace start, trace end) on s_tr
+
+        def mark(stream):
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            return e
 
         def create_async():
             tc = time.perf_counter()
+            e0 = mark(s_up)
             f = srt.Fields(phi_np, b_np, stream=s_up, async_=True, staged=True, pairs=args.pairs)
+            marks.append(("up", e0, mark(s_up)))
             call_ms.append(round((time.perf_counter() - tc) * 1e3, 1))
             return f
 
@@ -617,7 +625,9 @@ def run_ours(args):
                     nxt = create_async()
                     ev = torch.cuda.Event()
                     ev.record(s_up)
+                e0 = mark(s_tr)
                 cur.forward(nside, S, precision=args.precision, out=maps_h, stream=s_tr)
+                marks.append(("trace", e0, mark(s_tr)))
                 prev = cur
             prev.close()
             torch.cuda.synchronize()
@@ -627,13 +637,17 @@ def run_ours(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         del call_ms[:]
+        del marks[:]
         pipeline(K)
         pipe_s = max_over_ranks((time.perf_counter() - t0) / K, world)
+        # the timeline of the timed pipeline, ms from its first upload's start
+        base = marks[0][1]
+        timeline = [[kind, round(base.elapsed_time(a), 1), round(base.elapsed_time(b), 1)] for kind, a, b in marks]
         result["e2e"] = {"value": world * ray_steps / pipe_s, "unit": "ray-steps/s",
                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": pipe_s * 1e3,
                          "mode": "pipelined over %d steps: step i+1's upload (copy engines, high-priority stream) "
                                  "overlaps step i's trace; the first upload is inside the timed region" % K,
-                         "create_call_ms": call_ms}
+                         "create_call_ms": call_ms, "timeline_ms": timeline}
         result["e2e_serial"] = {"value": world * ray_steps / serial_s, "unit": "ray-steps/s",
                                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": serial_s * 1e3,
                                 "split_ms": {"fields_create_upload": float(sp[0]),
