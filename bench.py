@@ -84,7 +84,7 @@ def parse():
     ap.add_argument("--no-pairs", dest="pairs", action="store_false",
                     help="lay the fields out without their row-pair copies (SRT_FIELDS_NO_PAIRS): the packed MIXED "
                          "passes then form their tap pairs from the single layout")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--compare-batch", type=int, default=5, help="batch used for the FP64 / REF16 legs (-1: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--oracle-sample", type=int, default=3072,
@@ -599,10 +599,13 @@ def run_ours(args):
             e.record(stream)
             return e
 
-        def create_async():
+        def create_async(first=False):
+            # the first upload has no trace to hide behind: the layout kernel
+            # reads the pinned arrays itself, the fastest way in; the others go
+            # through the copy engines, which leave the SMs to the trace
             tc = time.perf_counter()
             e0 = mark(s_up)
-            f = srt.Fields(phi_np, b_np, stream=s_up, async_=True, staged=True, pairs=args.pairs)
+            f = srt.Fields(phi_np, b_np, stream=s_up, async_=True, staged=not first, pairs=args.pairs)
             marks.append(("up", e0, mark(s_up)))
             call_ms.append(round((time.perf_counter() - tc) * 1e3, 1))
             return f
@@ -611,7 +614,7 @@ def run_ours(args):
             # the previous step's fields are released before the next upload is
             # queued, so at most two sets (and the staging buffer) are held and
             # the memory pool reuses them instead of mapping new memory
-            nxt = create_async()
+            nxt = create_async(first=True)
             ev = torch.cuda.Event()
             ev.record(s_up)
             prev = None
@@ -646,7 +649,8 @@ def run_ours(args):
         result["e2e"] = {"value": world * ray_steps / pipe_s, "unit": "ray-steps/s",
                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": pipe_s * 1e3,
                          "mode": "pipelined over %d steps: step i+1's upload (copy engines, high-priority stream) "
-                                 "overlaps step i's trace; the first upload is inside the timed region" % K,
+                                 "overlaps step i's trace; the first upload (the layout kernel reading the pinned "
+                                 "arrays) is inside the timed region" % K,
                          "create_call_ms": call_ms, "timeline_ms": timeline}
         result["e2e_serial"] = {"value": world * ray_steps / serial_s, "unit": "ray-steps/s",
                                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": serial_s * 1e3,
