@@ -299,19 +299,17 @@ SRT_HD int wrap64(int64_t c, int n) {
   return (int)r;
 }
 
-// c mod n in [0, n): a float reciprocal for |c| < 2^24 (every finite ray
-// position), an integer modulo for anything else (e.g. a position made
-// non-finite by non-finite field values), so the result is always in range.
+// c mod n in [0, n) by a float reciprocal, exact for |c| < 2^24 (every
+// position FP32 resolves to a cell); any other c (a position made non-finite
+// by non-finite field values) is clamped into range, so every tap index stays
+// inside the array. Branch-free: selects only.
 SRT_HD int wrap32(int c, int n, float invn) {
   const int q = (int)floorf((float)c * invn);
-  int r = c - q * n;
-  if (r < 0) r += n;
-  if (r >= n) r -= n;
-  if (r < 0 || r >= n) {
-    r = c % n;
-    if (r < 0) r += n;
-  }
-  return r;
+  int r = (int)((unsigned)c - (unsigned)q * (unsigned)n);
+  r += r < 0 ? n : 0;
+  r -= r >= n ? n : 0;
+  r = r < 0 ? 0 : r;
+  return r >= n ? n - 1 : r;
 }
 
 SRT_HD int64_t cell_base(const Geom& G, int cx, int cy, int cz) {
@@ -771,9 +769,9 @@ struct MixedRay {
   float dn0[3];               // FP64 direction minus its FP32 base (for the extraction)
 };
 
-// (1 + q)^(-1/2) - 1 for |q| << 1 without cancellation.
+// (1 + q)^(-1/2) - 1 without cancellation, q > -1: -q / (s (1 + s)) with
+// s = (1 + q)^(1/2) (the numerator is q itself, the denominator ~2), no branch.
 SRT_HD float rsqrt1p_m1(float q) {
-  if (fabsf(q) < 1e-2f) return q * (-0.5f + q * (0.375f + q * (-0.3125f + q * 0.2734375f)));
   const float s = sqrtf(1.f + q);
   return -q / (s * (1.f + s));
 }
@@ -788,9 +786,12 @@ SRT_HD void unit_pert(const float* v0, const float* dv, float eta, float* D) {
 }
 
 // Quantities the B components contribute to the right-hand side
-// (snapshot-raytracer.cu:377-460), accumulated component by component.
+// (snapshot-raytracer.cu:377-460), accumulated component by component. With
+// G the matrix of B's gradients (row C = grad B_C), ngB = G^T n and
+// Gn = G n; the e.n.grad B scalars are e.G n / 2 + n.G e / 2
+// = e.(Gn + ngB) / 2, formed once from these two vectors.
 struct BAcc {
-  float val[3], ngB[3], e1ngB, e2ngB, nlap, T[6];
+  float val[3], ngB[3], Gn[3], nlap, T[6];
 };
 
 // B component C interpolated at the position staggered by -1/2 along axis C,
@@ -812,11 +813,7 @@ SRT_HD void add_b_component(const FieldPtrs& F, const Geom& G, const int* cc, co
                   C == 2 ? S : Cz, r);
   A.val[C] = r.v;
   for (int i = 0; i < 3; ++i) A.ngB[i] += r.g[i] * n[C];
-  const float gn = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
-  const float ga = r.g[0] * a[0] + r.g[1] * a[1] + r.g[2] * a[2];
-  const float gb = r.g[0] * b[0] + r.g[1] * b[1] + r.g[2] * b[2];
-  A.e1ngB += 0.5f * (a[C] * gn + n[C] * ga);
-  A.e2ngB += 0.5f * (b[C] * gn + n[C] * gb);
+  A.Gn[C] = r.g[0] * n[0] + r.g[1] * n[1] + r.g[2] * n[2];
   const float Hn[3] = {r.h[0] * n[0] + r.h[1] * n[1] + r.h[2] * n[2], r.h[1] * n[0] + r.h[3] * n[1] + r.h[4] * n[2],
                        r.h[2] * n[0] + r.h[4] * n[1] + r.h[5] * n[2]};
   // T_ij += n_C H_ij - 1/2 (delta_Ci (H n)_j + delta_Cj (H n)_i), ij in xx xy xz yy yz zz
@@ -906,7 +903,7 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   cr_weights_mixed(tc[2], Cz);
   BAcc A;
   A.ngB[0] = A.ngB[1] = A.ngB[2] = 0.f;
-  A.e1ngB = A.e2ngB = A.nlap = 0.f;
+  A.nlap = 0.f;
   for (int i = 0; i < 6; ++i) A.T[i] = 0.f;
   add_b_component<0, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
   add_b_component<1, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
@@ -927,11 +924,14 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   g[3] = v0 - n[0] * nv;
   g[4] = v1 - n[1] * nv;
   g[5] = v2 - n[2] * nv;
-  const float ag = a[0] * p.g[0] + a[1] * p.g[1] + a[2] * p.g[2];
-  const float bg = b[0] * p.g[0] + b[1] * p.g[1] + b[2] * p.g[2];
+  // 2 e.grad phi + e.n.grad B = e.(2 grad phi + (Gn + ngB) / 2)
+  float w[3];
+  for (int i = 0; i < 3; ++i) w[i] = 2.f * p.g[i] + 0.5f * (A.Gn[i] + A.ngB[i]);
+  const float aw = a[0] * w[0] + a[1] * w[1] + a[2] * w[2];
+  const float bw = b[0] * w[0] + b[1] * w[1] + b[2] * w[2];
   for (int i = 0; i < 3; ++i) {
-    g[6 + i] = -n[i] * (2.f * ag + A.e1ngB);
-    g[9 + i] = -n[i] * (2.f * bg + A.e2ngB);
+    g[6 + i] = -n[i] * aw;
+    g[9 + i] = -n[i] * bw;
   }
   const float L = n[0] * p.g[0] + n[1] * p.g[1] + n[2] * p.g[2] +
                   0.25f * (n[0] * A.ngB[0] + n[1] * A.ngB[1] + n[2] * A.ngB[2]);
@@ -942,29 +942,27 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   g[13] = -4.f * dAp * L - PH * dA + 0.5f * A.nlap * dA;
   float He[6];
   for (int i = 0; i < 6; ++i) He[i] = p.h[i] + 0.5f * A.T[i];
-  const float S1 = (a[0] * a[0] - b[0] * b[0]) * He[0] + (a[1] * a[1] - b[1] * b[1]) * He[3] +
-                   (a[2] * a[2] - b[2] * b[2]) * He[5] +
-                   2.f * ((a[0] * a[1] - b[0] * b[1]) * He[1] + (a[0] * a[2] - b[0] * b[2]) * He[2] +
-                          (a[1] * a[2] - b[1] * b[2]) * He[4]);
-  const float S2 = 2.f * (a[0] * b[0] * He[0] + a[1] * b[1] * He[3] + a[2] * b[2] * He[5]) +
-                   2.f * ((a[0] * b[1] + a[1] * b[0]) * He[1] + (a[0] * b[2] + a[2] * b[0]) * He[2] +
-                          (a[1] * b[2] + a[2] * b[1]) * He[4]);
+  // S1 = a.He a - b.He b, S2 = 2 a.He b (He symmetric)
+  const float Ha[3] = {He[0] * a[0] + He[1] * a[1] + He[2] * a[2], He[1] * a[0] + He[3] * a[1] + He[4] * a[2],
+                       He[2] * a[0] + He[4] * a[1] + He[5] * a[2]};
+  const float Hb[3] = {He[0] * b[0] + He[1] * b[1] + He[2] * b[2], He[1] * b[0] + He[3] * b[1] + He[4] * b[2],
+                       He[2] * b[0] + He[4] * b[1] + He[5] * b[2]};
+  const float S1 = (a[0] * Ha[0] + a[1] * Ha[1] + a[2] * Ha[2]) - (b[0] * Hb[0] + b[1] * Hb[1] + b[2] * Hb[2]);
+  const float S2 = 2.f * (a[0] * Hb[0] + a[1] * Hb[1] + a[2] * Hb[2]);
   const float dA2 = dA * dA;
   g[14] = 4.f * s1 * L + S1 * dA2;
   g[15] = 4.f * s2 * L + S2 * dA2;
-  // dA > 1/2  <=>  d12 > 1/2 - s (exact for the stage values of s)
-  if (d[12] > 0.5f - s) {
-    const float q = sqrtf(4.f + el1 * el1 + el2 * el2);
-    const float idA2 = 1.f / dA2;
-    g[13] += (s1 * s1 + s2 * s2) * idA2 / dA;
-    g[16] = -2.f * s1 * q * idA2;
-    g[17] = -2.f * s2 * q * idA2;
-    g[18] = -(s1 * el2 - s2 * el1) * idA2 / (2.f + q);
-  } else {
-    g[16] = 0.f;
-    g[17] = 0.f;
-    g[18] = 0.f;
-  }
+  // dA > 1/2  <=>  d12 > 1/2 - s (exact for the stage values of s); the
+  // branch's terms are formed either way and selected (no branch in the
+  // right-hand side; where dA = 0 they are not finite and not selected)
+  const bool on = d[12] > 0.5f - s;
+  const float q = sqrtf(4.f + el1 * el1 + el2 * el2);
+  const float idA2 = 1.f / dA2;
+  const float t13 = g[13] + (s1 * s1 + s2 * s2) * idA2 / dA;
+  g[13] = on ? t13 : g[13];
+  g[16] = on ? -2.f * s1 * q * idA2 : 0.f;
+  g[17] = on ? -2.f * s2 * q * idA2 : 0.f;
+  g[18] = on ? -(s1 * el2 - s2 * el1) * idA2 / (2.f + q) : 0.f;
 }
 
 // Number of leading state components accumulated with a compensation term
