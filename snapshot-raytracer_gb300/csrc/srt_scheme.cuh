@@ -228,10 +228,13 @@ struct SingleRows {
 // instruction): the x pass on rows y and y+1 at once with duplicated x
 // weights, the y pass with the weights of rows (0, 1) and (2, 3) (even / odd
 // partial sums). Per slice the six y sums are then completed (one add each)
-// and the z pass forms the ten outputs as five pairs that share an operand
-// pair: (v, gx) and (gz, hxz) from (a, ax), (hzz, gy) from (a, ay),
-// (hyz, hyy) from (ay, ayy), (hxx, hxy) from (axx, axy), so no lane of the
-// z pass is idle.
+// and the z pass forms the ten outputs as five pairs with no idle lane:
+// (v, gx), (gy, hyy) and (hxx, hxy) from the value weight on both lanes,
+// (gz, hxz) from the derivative weight on both, and (hyz, hzz) from the
+// (derivative, second-derivative) weight pair on (ay, a). Three weight pairs
+// and four operand pairs per slice: each output is still its own chain of
+// FMAs over the slices, so the results do not depend on the pairing, and this
+// one needs the fewest register copies to build the pairs.
 template <typename Rows>
 SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float>& Y, const CRW<float>& Z,
                           Tri<float>& r) {
@@ -245,8 +248,8 @@ SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float
   const float2 yg[2] = {make_float2(Y.g[0], Y.g[1]), make_float2(Y.g[2], Y.g[3])};
   const float2 yh[2] = {make_float2(Y.h[0], Y.h[1]), make_float2(Y.h[2], Y.h[3])};
   const float2 z0 = make_float2(0.f, 0.f);
-  // z-pass accumulators: (v, gx), (gz, hxz), (hzz, gy), (hyz, hyy), (hxx, hxy)
-  float2 VG0 = z0, G2H02 = z0, H22G1 = z0, H12H11 = z0, H00H01 = z0;
+  // z-pass accumulators: (v, gx), (gz, hxz), (gy, hyy), (hyz, hzz), (hxx, hxy)
+  float2 VG0 = z0, G2H02 = z0, G1H11 = z0, H12H22 = z0, H00H01 = z0;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     float2 A = z0, AY = z0, AYY = z0, AX = z0, AXY = z0, AXX = z0;
@@ -275,20 +278,20 @@ SRT_HD void tricubic_pair(const Rows& rows, const CRW<float>& X, const CRW<float
     const float zw = Z.w[c], zg = Z.g[c], zh = Z.h[c];
     VG0 = ffma2(dup2(zw), make_float2(a, ax), VG0);
     G2H02 = ffma2(dup2(zg), make_float2(a, ax), G2H02);
-    H22G1 = ffma2(make_float2(zh, zw), make_float2(a, ay), H22G1);
-    H12H11 = ffma2(make_float2(zg, zw), make_float2(ay, ayy), H12H11);
+    G1H11 = ffma2(dup2(zw), make_float2(ay, ayy), G1H11);
+    H12H22 = ffma2(make_float2(zg, zh), make_float2(ay, a), H12H22);
     H00H01 = ffma2(dup2(zw), make_float2(axx, axy), H00H01);
   }
   r.v = VG0.x;
   r.g[0] = VG0.y;
-  r.g[1] = H22G1.y;
+  r.g[1] = G1H11.x;
   r.g[2] = G2H02.x;
   r.h[0] = H00H01.x;
   r.h[1] = H00H01.y;
   r.h[2] = G2H02.y;
-  r.h[3] = H12H11.y;
-  r.h[4] = H12H11.x;
-  r.h[5] = H22G1.x;
+  r.h[3] = G1H11.y;
+  r.h[4] = H12H22.x;
+  r.h[5] = H12H22.y;
 }
 
 // ------------------------------------------------------------ cell lookup
