@@ -227,14 +227,11 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
   int q = (s1 - s0) * 4 - 1;
   float u[19];
   for (int j = 0; j < 19; ++j) u[j] = ld_stream(tape + ((int64_t)(q >> 2) * kTapeStep + 19 * (q & 3) + j) * A.count);
-  float an[19];  // a of the stage after this one
+  float an[19];  // a of the stage after this one (finite; its weight is 0 at stage 3)
+  for (int j = 0; j < 19; ++j) an[j] = 0.f;
 #pragma unroll 1
   for (; q >= 0; --q) {
     const int st = s0 + (q >> 2), stage = q & 3;
-    if (stage == 3) {
-      for (int j = 0; j < 19; ++j) s_tot[j][t] = 0.f;
-      for (int j = 0; j < 19; ++j) an[j] = 0.f;
-    }
     const float c = (stage == 0) ? 0.f : ((stage == 3) ? 1.f : 0.5f);
     const float wl = (stage == 0 || stage == 3) ? (1.f / 6.f) : (1.f / 3.f);
     const float wa = (stage == 3) ? 0.f : ((stage == 2) ? 1.f : 0.5f);
@@ -242,13 +239,14 @@ __device__ __forceinline__ void sweep_segment(const AdjArgs& A, int sgi, int64_t
     for (int j = 0; j < 19; ++j) fb[j] = wl * s_lam[j][t] + wa * an[j];
     StageView<float> V;
     stage_view_mixed(u, (float)st + c, R, A.G, x0, V);
-    if (q > 0) {  // prefetch the next (earlier) stage's inputs
-      const int qn = q - 1;
+    {  // prefetch the next (earlier) stage's inputs (the last stage reloads its own)
+      const int qn = q > 0 ? q - 1 : 0;
       for (int j = 0; j < 19; ++j) u[j] = ld_stream(tape + ((int64_t)(qn >> 2) * kTapeStep + 19 * (qn & 3) + j) * A.count);
     }
     for (int j = 0; j < 19; ++j) an[j] = 0.f;
     rhs_vjp<float, AccB, AccP, PAIR>(V, A.F, A.G, fb, an, accb, accp);
-    for (int j = 0; j < 19; ++j) s_tot[j][t] += an[j];
+    // the step's running sum of the a's restarts at its last stage
+    for (int j = 0; j < 19; ++j) s_tot[j][t] = (stage == 3 ? 0.f : s_tot[j][t]) + an[j];
     if (stage == 0)
       for (int j = 0; j < 19; ++j) s_lam[j][t] += s_tot[j][t];
   }

@@ -480,29 +480,36 @@ SRT_HD void rhs_vjp(const StageView<T>& V, const FieldPtrs& F, const Geom& G, co
   const T PHb = -V.A * fb[13];
   const T nlapb = T(0.5) * V.A * fb[13];
   const T S1b = V.A * V.A * fb[14], S2b = V.A * V.A * fb[15];
+  // the dA > 1/2 branch's terms, formed either way and selected (no branch;
+  // where dA = 0 they are not finite and not selected)
   T Ab = 0, s1b = 0, s2b = 0, el1b = 0, el2b = 0;
-  if (V.branch) {
+  {
     const T A2 = V.A * V.A, A3 = A2 * V.A;
     const T q = sqrt(T(4) + V.e1 * V.e1 + V.e2 * V.e2);
-    s1b += T(2) * V.s1 / A3 * fb[13];
-    s2b += T(2) * V.s2 / A3 * fb[13];
-    Ab += T(-3) * (V.s1 * V.s1 + V.s2 * V.s2) / (A3 * V.A) * fb[13];
-    s1b += T(-2) * q / A2 * fb[16];
+    T bs1 = T(2) * V.s1 / A3 * fb[13];
+    T bs2 = T(2) * V.s2 / A3 * fb[13];
+    T bA = T(-3) * (V.s1 * V.s1 + V.s2 * V.s2) / (A3 * V.A) * fb[13];
+    bs1 += T(-2) * q / A2 * fb[16];
     T qb = T(-2) * V.s1 / A2 * fb[16];
-    Ab += T(4) * V.s1 * q / A3 * fb[16];
-    s2b += T(-2) * q / A2 * fb[17];
+    bA += T(4) * V.s1 * q / A3 * fb[16];
+    bs2 += T(-2) * q / A2 * fb[17];
     qb += T(-2) * V.s2 / A2 * fb[17];
-    Ab += T(4) * V.s2 * q / A3 * fb[17];
+    bA += T(4) * V.s2 * q / A3 * fb[17];
     const T D = A2 * (T(2) + q), N = V.s1 * V.e2 - V.s2 * V.e1;
     const T Nb = -fb[18] / D, Db = N * fb[18] / (D * D);
-    s1b += V.e2 * Nb;
-    el2b += V.s1 * Nb;
-    s2b += -V.e1 * Nb;
-    el1b += -V.s2 * Nb;
-    Ab += T(2) * V.A * (T(2) + q) * Db;
+    bs1 += V.e2 * Nb;
+    T be2 = V.s1 * Nb;
+    bs2 += -V.e1 * Nb;
+    T be1 = -V.s2 * Nb;
+    bA += T(2) * V.A * (T(2) + q) * Db;
     qb += A2 * Db;
-    el1b += V.e1 / q * qb;
-    el2b += V.e2 / q * qb;
+    be1 += V.e1 / q * qb;
+    be2 += V.e2 / q * qb;
+    s1b = V.branch ? bs1 : T(0);
+    s2b = V.branch ? bs2 : T(0);
+    Ab = V.branch ? bA : T(0);
+    el1b = V.branch ? be1 : T(0);
+    el2b = V.branch ? be2 : T(0);
   }
   // cotangent of the effective tidal matrix He = H + T/2 (full symmetric)
   T Heb[6];
