@@ -458,22 +458,22 @@ SRT_HD void rhs_finish(const R* y, const R* n, const R* a, const R* b, const BSu
                            (a[1] * b[2] + a[2] * b[1]) * He[4]);
   dy[14] = 4.0 * s1 * L + S1 * dA * dA;
   dy[15] = 4.0 * s2 * L + S2 * dA * dA;
-  if (dA > 0.5) {
-    const R dA2 = dA * dA;
-    const R q = sqrt_r(4.0 + el1 * el1 + el2 * el2);
-    const R num[4] = {s1 * s1 + s2 * s2, -2.0 * s1 * q, -2.0 * s2 * q, -(s1 * el2 - s2 * el1)};
-    const R den[4] = {dA2 * dA, dA2, dA2, dA2 * (2.0 + q)};
-    R quo[4];
-    div(num, den, quo);
-    dy[13] += quo[0];
-    dy[16] = quo[1];
-    dy[17] = quo[2];
-    dy[18] = quo[3];
-  } else {
-    dy[16] = 0.0;
-    dy[17] = 0.0;
-    dy[18] = 0.0;
-  }
+  // the dA > 1/2 branch's terms, formed either way and selected (the same
+  // operations when it is taken; where dA = 0 they are not finite and not
+  // selected)
+  const bool on = dA > 0.5;
+  const R dA2 = dA * dA;
+  const R q = sqrt_r(4.0 + el1 * el1 + el2 * el2);
+  const R num[4] = {s1 * s1 + s2 * s2, -2.0 * s1 * q, -2.0 * s2 * q, -(s1 * el2 - s2 * el1)};
+  const R den[4] = {dA2 * dA, dA2, dA2, dA2 * (2.0 + q)};
+  R quo[4];
+  div(num, den, quo);
+  const R zero(0.0);
+  const R t13 = dy[13] + quo[0];
+  dy[13] = on ? t13 : dy[13];
+  dy[16] = on ? quo[1] : zero;
+  dy[17] = on ? quo[2] : zero;
+  dy[18] = on ? quo[3] : zero;
 }
 
 // 19-component right-hand side on the full state y (FP64 or REF16 arithmetic).
@@ -759,7 +759,8 @@ SRT_HD void locate_mixed(float th, float lo, int n, float invn, int& cc, float& 
   tc = u + e;
   const float v = (u - 0.5f) + e;   // frac(x) - 1/2 (u - 1/2 exact for u >= 1/4)
   const int c = (int)fl + (int)k;
-  cc = (unsigned)c < (unsigned)n ? c : wrap32(c, n, invn);
+  const int cw = wrap32(c, n, invn);  // formed either way: a select, not a branch
+  cc = (unsigned)c < (unsigned)n ? c : cw;
   const bool up = v >= 0.f;  // x - 1/2 lies in the same cell
   ts = up ? v : v + 1.f;
   cs = up ? cc : (cc == 0 ? n - 1 : cc - 1);
@@ -899,7 +900,9 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
     const float lo = (tl - pe) + d[i];
     locate_mixed(th, lo, G.n[i], G.invn[i], cc[i], tc[i], cs[i], ts[i], df[i]);
   }
-  gd.face(fminf(fminf(df[0], df[1]), df[2]));
+  // at s = 0 the ray sits exactly on the observer (a grid node, offsets
+  // exactly 0) in both precisions, so no cell choice can differ there
+  gd.face(s > 0.f ? fminf(fminf(df[0], df[1]), df[2]) : 1.f);
   CRW<float> Cx, Cy, Cz;  // centred weights, shared by phi and two axes of each B component
   cr_weights_mixed(tc[0], Cx);
   cr_weights_mixed(tc[1], Cy);
@@ -1041,19 +1044,18 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
     if (us)
       for (int j = 0; j < 19; ++j) st_stream(us + (19 * st + j) * stride, ys[j]);
     rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k, gd);
-    // at s = 0 the ray sits exactly on the observer (a grid node, offsets
-    // exactly 0) in both precisions, so no cell choice can differ there
-    if (step == 0 && st == 0 && gd.m) gd.m[1] = 1.f;
-    if (st == 0) {
-      for (int j = 0; j < 19; ++j) acc[j] = k[j];
-    } else if (st < 3) {
+    {  // acc = k1 + 2 k2 + 2 k3 by selects (stage 4's k is added at the update):
+       // the same FMAs where a stage adds, exact no-ops where it does not
+      const float w = st == 0 ? 1.f : (st < 3 ? 2.f : 0.f);
+      const bool first = st == 0;
 #pragma unroll
       for (int j = 0; j < 18; j += 2) {
-        const float2 r = ffma2(dup2(2.f), make_float2(k[j], k[j + 1]), make_float2(acc[j], acc[j + 1]));
+        const float2 r = ffma2(dup2(w), make_float2(k[j], k[j + 1]),
+                               make_float2(first ? 0.f : acc[j], first ? 0.f : acc[j + 1]));
         acc[j] = r.x;
         acc[j + 1] = r.y;
       }
-      acc[18] += 2.f * k[18];
+      acc[18] = w * k[18] + (first ? 0.f : acc[18]);
     }
   }
   // y += (k1 + 2 k2 + 2 k3 + k4) / 6 with the rounding error of each sum kept
