@@ -283,12 +283,13 @@ def test_single_layout_packed_path_equals_pair_layout(srt):
     """The MIXED forward and vjp read their packed tap pairs either from the
     row-pair copy of the fields or, with SRT_FIELDS_NO_PAIRS, from the single
     halo layout (two loads per pair): the float2 values and the packed
-    operations are the same, so the maps, the refined-ray counts and the
-    deterministic phi gradient agree bit for bit. The B components' tap
-    cotangents come from scalar FP32 expressions the compiler may round in a
-    different order in the two kernel variants: measured one float ulp on
-    ~0.5 % of the B gradient entries, so those are compared to 1e-6 of the
-    largest entry."""
+    operations are the same, so the maps and the refined-ray counts agree bit
+    for bit. The sweep's B passes form their tap cotangents and their share of
+    the state cotangent from scalar FP32 expressions the compiler may round in
+    a different order in the two kernel variants (one float ulp on ~0.5 % of
+    the B gradient entries); that state cotangent feeds the phi scatter of the
+    earlier stages, so both gradients are compared to 1e-6 of their largest
+    entry."""
     import srt_fields
 
     phi, b = srt_fields.gaussian_fields_np(48, seed=17)
@@ -302,9 +303,10 @@ def test_single_layout_packed_path_equals_pair_layout(srt):
             out[pairs] = (m, st.refined_rays, g, gb)
     assert np.array_equal(out[True][0].view(np.uint32), out[False][0].view(np.uint32))
     assert out[True][1] == out[False][1]
-    assert np.array_equal(out[True][2].view(np.uint32), out[False][2].view(np.uint32))
-    gb_p, gb_s = out[True][3], out[False][3]
-    assert np.abs(gb_p - gb_s).max() <= 1e-6 * np.abs(gb_p).max()
+    for k in (2, 3):
+        a, c = out[True][k], out[False][k]
+        err = np.abs(a - c).max() / np.abs(a).max()
+        assert err <= 1e-6, ("phi" if k == 2 else "B", err)
 
 
 @pytest.mark.parametrize("extents", [(24, 24, 24), (5, 3, 4)])
