@@ -84,7 +84,9 @@ def parse():
     ap.add_argument("--no-pairs", dest="pairs", action="store_false",
                     help="lay the fields out without their row-pair copies (SRT_FIELDS_NO_PAIRS): the packed MIXED "
                          "passes then form their tap pairs from the single layout")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=7,
+                    help="timed snapshots of the pipelined end-to-end leg, less one (the serial leg times "
+                         "min(this, 3)); 0 skips both")
     ap.add_argument("--compare-batch", type=int, default=5, help="batch used for the FP64 / REF16 legs (-1: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU-baseline sample")
     ap.add_argument("--oracle-sample", type=int, default=3072,
@@ -565,7 +567,7 @@ def run_ours(args):
         # (the layout kernel reads the pinned memory directly), traces, reads
         # the maps back and releases the fields
         times, split = [], []
-        for i in range(args.e2e_steps + 1):
+        for i in range(min(args.e2e_steps, 3) + 1):
             barrier(world)
             torch.cuda.synchronize()
             t0 = time.perf_counter()

@@ -323,6 +323,25 @@ __device__ __forceinline__ void step_dd_group(const FieldPtrs& F, const Geom& G,
   for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
 }
 
+// step_dd_group with the state and the RK4 accumulator in shared memory, one
+// copy per lane group (the four lanes of a group form the same values, so
+// each writes what the others write): the registers then hold only the stage
+// input, the stage's k and the right-hand side's working set.
+__device__ __forceinline__ void step_dd_group_sm(const FieldPtrs& F, const Geom& G, dd* y, dd* acc, int field,
+                                                 int group, unsigned mask) {
+  dd k[19];
+#pragma unroll 1
+  for (int st = 0; st < 4; ++st) {
+    const float c = (st == 3) ? 1.f : 0.5f;
+    dd ys[19];
+    for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
+    rhs_dd_group(ys, k, F, G, field, group, mask);
+    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
+  }
+  const dd sixth = dd(1.0 / 6.0);
+  for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
+}
+
 // step_dd_group with one lane doing the whole ray (rhs_dd: all four
 // interpolations and the right-hand side once).
 __device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, dd* y) {
@@ -350,8 +369,12 @@ __device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, dd* 
 //     on each lane (~48k against ~28k FP32 instructions per ray and stage).
 // The environment variables SRT_REFINE_DD_MIN and SRT_REFINE_WIDE_MIN override
 // dd_min and wide_min (tests use them to reach every path on small skies).
+// The double-float four-lane groups keep their state in shared memory and fit
+// 12 one-warp blocks per SM (168 registers, no spill): the ~1,550 warps of a
+// 1024^3 sky's list then run in one wave instead of two (113 against 157 ms).
 template <int MODE>
-__global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t dd_min, int64_t wide_min) {
+__global__ void __launch_bounds__(32, MODE == 1 ? 12 : 1)
+    refine_kernel(const TraceArgs A, int64_t dd_min, int64_t wide_min) {
   constexpr int LANES = MODE == 2 ? 1 : 4;
   constexpr int kRays = 32 / LANES;  // rays per warp
   const int lane = threadIdx.x;
@@ -383,13 +406,23 @@ __global__ void __launch_bounds__(32) refine_kernel(const TraceArgs A, int64_t d
       for (int step = 0; step < A.n_steps; ++step) step_dd1(A.F, A.G, y);
       extract_dd(d, A.G, y, out);
     } else {
-      dd y[19];
-      init_dd(d, A.G, y);
+      __shared__ dd s_y[8][19], s_acc[8][19];
+      dd* y = s_y[lane >> 2];
+      {
+        dd yl[19];
+        init_dd(d, A.G, yl);
+        for (int j = 0; j < 19; ++j) y[j] = yl[j];
+      }
       const int64_t live = min((int64_t)kRays, n - k0);
       const unsigned mask = (live >= kRays) ? 0xffffffffu : ((1u << (4 * live)) - 1u);
 #pragma unroll 1
-      for (int step = 0; step < A.n_steps; ++step) step_dd_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
-      extract_dd(d, A.G, y, out);
+      for (int step = 0; step < A.n_steps; ++step)
+        step_dd_group_sm(A.F, A.G, y, s_acc[lane >> 2], lane & 3, lane & ~3, mask);
+      {
+        dd yl[19];
+        for (int j = 0; j < 19; ++j) yl[j] = y[j];
+        extract_dd(d, A.G, yl, out);
+      }
     }
     if (lane % LANES == 0) {
 #pragma unroll
