@@ -344,8 +344,15 @@ __device__ __forceinline__ void step_dd_group_sm(const FieldPtrs& F, const Geom&
 
 // step_dd_group with one lane doing the whole ray (rhs_dd: all four
 // interpolations and the right-hand side once).
-__device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, dd* y) {
-  dd acc[19], k[19], ys[19];
+// One lane's double-float state in a shared-memory column of a warp's array
+// (component j at c[32 j]).
+struct DdCol {
+  dd* c;
+  __device__ dd& operator[](int j) const { return c[32 * j]; }
+};
+
+__device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, const DdCol& y, const DdCol& acc) {
+  dd k[19], ys[19];
 #pragma unroll 1
   for (int st = 0; st < 4; ++st) {
     const float c = (st == 3) ? 1.f : 0.5f;
@@ -369,11 +376,12 @@ __device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, dd* 
 //     on each lane (~48k against ~28k FP32 instructions per ray and stage).
 // The environment variables SRT_REFINE_DD_MIN and SRT_REFINE_WIDE_MIN override
 // dd_min and wide_min (tests use them to reach every path on small skies).
-// The double-float four-lane groups keep their state in shared memory and fit
-// 12 one-warp blocks per SM (168 registers, no spill): the ~1,550 warps of a
-// 1024^3 sky's list then run in one wave instead of two (113 against 157 ms).
+// The double-float re-traces keep their state in shared memory and fit 12
+// one-warp blocks per SM (168 registers, no spill): the ~1,550 four-lane warps
+// of a 1024^3 sky's list then run in one wave instead of two (113 against
+// 157 ms); the one-lane warps of a 2048^3 sky's ~245k rays gain 0.8 % of the sky.
 template <int MODE>
-__global__ void __launch_bounds__(32, MODE == 1 ? 12 : 1)
+__global__ void __launch_bounds__(32, (MODE == 1 || MODE == 2) ? 12 : 1)
     refine_kernel(const TraceArgs A, int64_t dd_min, int64_t wide_min) {
   constexpr int LANES = MODE == 2 ? 1 : 4;
   constexpr int kRays = 32 / LANES;  // rays per warp
@@ -400,11 +408,20 @@ __global__ void __launch_bounds__(32, MODE == 1 ? 12 : 1)
       for (int step = 0; step < A.n_steps; ++step) step_fp64_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
       extract_std(d, A.G, y, out);
     } else if (MODE == 2) {
-      dd y[19];
-      init_dd(d, A.G, y);
+      __shared__ dd s_y1[19][32], s_acc1[19][32];
+      const DdCol y{&s_y1[0][lane]}, acc{&s_acc1[0][lane]};
+      {
+        dd yl[19];
+        init_dd(d, A.G, yl);
+        for (int j = 0; j < 19; ++j) y[j] = yl[j];
+      }
 #pragma unroll 1
-      for (int step = 0; step < A.n_steps; ++step) step_dd1(A.F, A.G, y);
-      extract_dd(d, A.G, y, out);
+      for (int step = 0; step < A.n_steps; ++step) step_dd1(A.F, A.G, y, acc);
+      {
+        dd yl[19];
+        for (int j = 0; j < 19; ++j) yl[j] = y[j];
+        extract_dd(d, A.G, yl, out);
+      }
     } else {
       __shared__ dd s_y[8][19], s_acc[8][19];
       dd* y = s_y[lane >> 2];
