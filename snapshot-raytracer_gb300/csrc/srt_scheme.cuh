@@ -1035,7 +1035,7 @@ template <bool PAIR = false>
 SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, const float* x0, int step, float* y,
                        float* us, int64_t stride, Guard& gd) {
   float k[19], acc[19], ys[19];
-  for (int j = 0; j < 19; ++j) k[j] = 0.f;
+  for (int j = 0; j < 19; ++j) k[j] = acc[j] = 0.f;
   const float s0 = (float)step;
 #pragma unroll 1
   for (int st = 0; st < 4; ++st) {
@@ -1044,18 +1044,17 @@ SRT_HD void step_mixed(const MixedRay& R, const FieldPtrs& F, const Geom& G, con
     if (us)
       for (int j = 0; j < 19; ++j) st_stream(us + (19 * st + j) * stride, ys[j]);
     rhs_mixed<PAIR>(ys, s0 + c, R, F, G, x0, k, gd);
-    {  // acc = k1 + 2 k2 + 2 k3 by selects (stage 4's k is added at the update):
-       // the same FMAs where a stage adds, exact no-ops where it does not
+    {  // acc = k1 + 2 k2 + 2 k3 with weights 1, 2, 2, 0 on a zeroed accumulator
+       // (stage 4's k is added at the update): the same FMAs where a stage
+       // adds, exact no-ops where it does not, and no branch
       const float w = st == 0 ? 1.f : (st < 3 ? 2.f : 0.f);
-      const bool first = st == 0;
 #pragma unroll
       for (int j = 0; j < 18; j += 2) {
-        const float2 r = ffma2(dup2(w), make_float2(k[j], k[j + 1]),
-                               make_float2(first ? 0.f : acc[j], first ? 0.f : acc[j + 1]));
+        const float2 r = ffma2(dup2(w), make_float2(k[j], k[j + 1]), make_float2(acc[j], acc[j + 1]));
         acc[j] = r.x;
         acc[j + 1] = r.y;
       }
-      acc[18] = w * k[18] + (first ? 0.f : acc[18]);
+      acc[18] = w * k[18] + acc[18];
     }
   }
   // y += (k1 + 2 k2 + 2 k3 + k4) / 6 with the rounding error of each sum kept
