@@ -19,6 +19,7 @@
 //     the effective tidal matrix) are added after the four passes.
 // Catmull-Rom's third derivative is piecewise constant: weights (-3, 9, -9, 3).
 #pragma once
+#include <type_traits>
 #include "srt_scheme.cuh"
 
 namespace srt {
@@ -269,9 +270,18 @@ SRT_HD void tricubic_vjp_pair(const Rows& rows, int64_t base, int64_t px, int64_
     Bg[pr] = fmul2(dup2(qb[6]), yw[pr]);
     Ah[pr] = fmul2(dup2(qb[4]), yw[pr]);
   }
+  // z pass (and an unconditional prefetch): packed for the passes without a
+  // scatter (they have the registers to spare), on the operand pairs the y
+  // sums form: value weight (o000, o100)
+  // (o010, o110) (o020, o120) (o200, o210) (o030, o300), derivative weight
+  // (o001, o101) (o011, o111) (o021, -) (o201, -), second derivative
+  // (o002, o102) (o012, -), third (o003, -); scalar where the scatter's
+  // working set is live. Every output is the same FMA chain over the slices.
+  constexpr bool kPackedZ = std::is_same<Acc, AccNone>::value;
   float o000 = 0, o001 = 0, o002 = 0, o003 = 0, o010 = 0, o011 = 0, o012 = 0, o020 = 0, o021 = 0, o030 = 0;
   float o100 = 0, o101 = 0, o102 = 0, o110 = 0, o111 = 0, o120 = 0, o200 = 0, o201 = 0, o210 = 0, o300 = 0;
   const float2 z0 = make_float2(0.f, 0.f);
+  float2 W0 = z0, W1 = z0, W2 = z0, W3 = z0, W4 = z0, G0 = z0, G1 = z0, G2 = z0, G3 = z0, H0 = z0, H1 = z0, K0 = z0;
   // taps of the next slice, loaded while the current one is processed
   float2 nt[8];
   for (int pr = 0; pr < 2; ++pr)
@@ -288,9 +298,14 @@ SRT_HD void tricubic_vjp_pair(const Rows& rows, int64_t base, int64_t px, int64_
     const float2 zw = dup2(zwc), zg = dup2(zgc), zh = dup2(zhc);
     float2 ct[8];
     for (int i = 0; i < 8; ++i) ct[i] = nt[i];
-    if (c < 3)
+    if constexpr (kPackedZ) {  // the last slice reloads itself: no branch in the loop
+      const int cn = c < 3 ? c + 1 : 3;
+      for (int pr = 0; pr < 2; ++pr)
+        for (int i = 0; i < 4; ++i) nt[4 * pr + i] = rows(cn, pr, i);
+    } else if (c < 3) {  // (fewer registers where the scatter's working set is live)
       for (int pr = 0; pr < 2; ++pr)
         for (int i = 0; i < 4; ++i) nt[4 * pr + i] = rows(c + 1, pr, i);
+    }
 #pragma unroll
     for (int pr = 0; pr < 2; ++pr) {
       const float2 t0 = ct[4 * pr], t1 = ct[4 * pr + 1], t2 = ct[4 * pr + 2], t3 = ct[4 * pr + 3];
@@ -328,19 +343,43 @@ SRT_HD void tricubic_vjp_pair(const Rows& rows, int64_t base, int64_t px, int64_
         acc.add_row(row + px, v[0].y, v[1].y, v[2].y, v[3].y);
       }
     }
-    const float S00 = s00.x + s00.y, S01 = s01.x + s01.y, S02 = s02.x + s02.y, S03 = s03.x + s03.y;
-    const float S10 = s10.x + s10.y, S11 = s11.x + s11.y, S12 = s12.x + s12.y;
-    const float S20 = s20.x + s20.y, S21 = s21.x + s21.y, S30 = s30.x + s30.y;
-    o000 += zwc * S00; o001 += zgc * S00; o002 += zhc * S00; o003 += zkc * S00;
-    o010 += zwc * S01; o011 += zgc * S01; o012 += zhc * S01;
-    o020 += zwc * S02; o021 += zgc * S02;
-    o030 += zwc * S03;
-    o100 += zwc * S10; o101 += zgc * S10; o102 += zhc * S10;
-    o110 += zwc * S11; o111 += zgc * S11;
-    o120 += zwc * S12;
-    o200 += zwc * S20; o201 += zgc * S20;
-    o210 += zwc * S21;
-    o300 += zwc * S30;
+    if constexpr (kPackedZ) {
+      const float2 P0 = make_float2(s00.x + s00.y, s10.x + s10.y), P1 = make_float2(s01.x + s01.y, s11.x + s11.y);
+      const float2 P2 = make_float2(s02.x + s02.y, s12.x + s12.y), P3 = make_float2(s20.x + s20.y, s21.x + s21.y);
+      const float2 P4 = make_float2(s03.x + s03.y, s30.x + s30.y);
+      W0 = ffma2(zw, P0, W0);
+      W1 = ffma2(zw, P1, W1);
+      W2 = ffma2(zw, P2, W2);
+      W3 = ffma2(zw, P3, W3);
+      W4 = ffma2(zw, P4, W4);
+      G0 = ffma2(zg, P0, G0);
+      G1 = ffma2(zg, P1, G1);
+      G2 = ffma2(zg, P2, G2);
+      G3 = ffma2(zg, P3, G3);
+      H0 = ffma2(zh, P0, H0);
+      H1 = ffma2(zh, P1, H1);
+      K0 = ffma2(dup2(zkc), P0, K0);
+    } else {
+      const float S00 = s00.x + s00.y, S01 = s01.x + s01.y, S02 = s02.x + s02.y, S03 = s03.x + s03.y;
+      const float S10 = s10.x + s10.y, S11 = s11.x + s11.y, S12 = s12.x + s12.y;
+      const float S20 = s20.x + s20.y, S21 = s21.x + s21.y, S30 = s30.x + s30.y;
+      o000 += zwc * S00; o001 += zgc * S00; o002 += zhc * S00; o003 += zkc * S00;
+      o010 += zwc * S01; o011 += zgc * S01; o012 += zhc * S01;
+      o020 += zwc * S02; o021 += zgc * S02;
+      o030 += zwc * S03;
+      o100 += zwc * S10; o101 += zgc * S10; o102 += zhc * S10;
+      o110 += zwc * S11; o111 += zgc * S11;
+      o120 += zwc * S12;
+      o200 += zwc * S20; o201 += zgc * S20;
+      o210 += zwc * S21;
+      o300 += zwc * S30;
+    }
+  }
+  if constexpr (kPackedZ) {
+    o000 = W0.x, o100 = W0.y, o010 = W1.x, o110 = W1.y, o020 = W2.x, o120 = W2.y;
+    o200 = W3.x, o210 = W3.y, o030 = W4.x, o300 = W4.y;
+    o001 = G0.x, o101 = G0.y, o011 = G1.x, o111 = G1.y, o021 = G2.x, o201 = G3.x;
+    o002 = H0.x, o102 = H0.y, o012 = H1.x, o003 = K0.x;
   }
   Q.v = o000;
   Q.g[0] = o100;
