@@ -408,8 +408,10 @@ __global__ void __launch_bounds__(32, (MODE == 1 || MODE == 2) ? 12 : 1)
       for (int step = 0; step < A.n_steps; ++step) step_fp64_group(A.F, A.G, y, lane & 3, lane & ~3, mask);
       extract_std(d, A.G, y, out);
     } else if (MODE == 2) {
-      __shared__ dd s_y1[19][32], s_acc1[19][32];
-      const DdCol y{&s_y1[0][lane]}, acc{&s_acc1[0][lane]};
+      // raw storage viewed as dd (two floats, as float2): a shared array of a
+      // type with a constructor would not be initialised anyway
+      __shared__ float2 s_y1[19][32], s_acc1[19][32];
+      const DdCol y{reinterpret_cast<dd*>(&s_y1[0][lane])}, acc{reinterpret_cast<dd*>(&s_acc1[0][lane])};
       {
         dd yl[19];
         init_dd(d, A.G, yl);
@@ -423,8 +425,8 @@ __global__ void __launch_bounds__(32, (MODE == 1 || MODE == 2) ? 12 : 1)
         extract_dd(d, A.G, yl, out);
       }
     } else {
-      __shared__ dd s_y[8][19], s_acc[8][19];
-      dd* y = s_y[lane >> 2];
+      __shared__ float2 s_y[8][19], s_acc[8][19];  // dd storage, as above
+      dd* y = reinterpret_cast<dd*>(s_y[lane >> 2]);
       {
         dd yl[19];
         init_dd(d, A.G, yl);
@@ -434,7 +436,7 @@ __global__ void __launch_bounds__(32, (MODE == 1 || MODE == 2) ? 12 : 1)
       const unsigned mask = (live >= kRays) ? 0xffffffffu : ((1u << (4 * live)) - 1u);
 #pragma unroll 1
       for (int step = 0; step < A.n_steps; ++step)
-        step_dd_group_sm(A.F, A.G, y, s_acc[lane >> 2], lane & 3, lane & ~3, mask);
+        step_dd_group_sm(A.F, A.G, y, reinterpret_cast<dd*>(s_acc[lane >> 2]), lane & 3, lane & ~3, mask);
       {
         dd yl[19];
         for (int j = 0; j < 19; ++j) yl[j] = y[j];
