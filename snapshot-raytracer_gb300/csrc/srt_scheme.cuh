@@ -758,7 +758,9 @@ SRT_HD void locate_mixed(float th, float lo, int n, float invn, int& cc, float& 
   e += s - (u + k);
   tc = u + e;
   const float v = (u - 0.5f) + e;   // frac(x) - 1/2 (u - 1/2 exact for u >= 1/4)
-  const int c = (int)fl + (int)k;
+  // (summed as unsigned: a non-finite position converts to any int, and the
+  // cell is then only required to land in range)
+  const int c = (int)((unsigned)(int)fl + (unsigned)(int)k);
   const int cw = wrap32(c, n, invn);  // formed either way: a select, not a branch
   cc = (unsigned)c < (unsigned)n ? c : cw;
   const bool up = v >= 0.f;  // x - 1/2 lies in the same cell

@@ -122,3 +122,16 @@ def test_far_outside_the_box(loc):
             th = np.float32(rng.choice([-1.0, 1.0]) * 10.0 ** rng.uniform(1, 6.5))
             lo = np.float32(rng.standard_normal() * 1e-3)
             check(loc, th, lo, n)
+
+
+def test_unresolvable_and_non_finite_positions_stay_in_range(loc):
+    """Positions beyond 2^24 cells (where FP32 no longer resolves a cell) and
+    non-finite positions (non-finite field values) still give cells inside
+    the grid, so every tap index stays inside the halo-padded arrays; the wrap
+    is exact below 2^24 cells (test_far_outside_the_box)."""
+    inf, nan = float("inf"), float("nan")
+    for n in (16, 1000, 1024):
+        for th in (3e7, -3e7, 3e9, -3e9, 1e38, -1e38, inf, -inf, nan):
+            for lo in (0.0, 1e-3, -1e-3, nan):
+                cc, tc, cs, ts, df = loc(th, lo, n)
+                assert 0 <= cc < n and 0 <= cs < n, (th, lo, n, cc, cs)
