@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SRT_ABI_VERSION 3
+#define SRT_ABI_VERSION 4
 
 /* status codes */
 #define SRT_OK 0
@@ -102,6 +102,8 @@ typedef struct srt_stats {
   int64_t h2d_bytes;   /* bytes copied host -> device by this call */
   int64_t d2h_bytes;   /* bytes copied device -> host by this call */
   int64_t refined_rays; /* MIXED: rays re-traced in FP64 (synchronous calls) */
+  double retrace_ms;    /* srt_forward, MIXED: the re-trace launches' share of trace_ms
+                           (synchronous calls; 0 elsewhere). Added in ABI version 4. */
 } srt_stats;
 
 /* ---------------------------------------------------------------- library */

@@ -442,7 +442,7 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
   float* dmaps = nullptr;
   int64_t* refine_list = nullptr;
   unsigned long long* refine_count = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, em = nullptr;
   int64_t kernels = 0;
   int prev = 0;
   cudaGetDevice(&prev);
@@ -500,10 +500,12 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     if (timed) {
       SRT_CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
       SRT_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+      SRT_CUDA_TRY(cudaEventCreate(&em), "cudaEventCreate");
       SRT_CUDA_TRY(cudaEventRecord(e0, s), "cudaEventRecord");
     }
     const int kmode = (precision == SRT_PRECISION_MIXED && f->pr[0]) ? kMIXED_PAIR : precision;
     SRT_CUDA_TRY(launch_trace(kmode, a, s, &kernels), "trace kernel launch");
+    if (timed) SRT_CUDA_TRY(cudaEventRecord(em, s), "cudaEventRecord");  // trace kernel done
     if (refine) SRT_CUDA_TRY(launch_refine(a, s, &kernels), "refine kernel launch");
     if (timed) SRT_CUDA_TRY(cudaEventRecord(e1, s), "cudaEventRecord");
     if (!dev_out) {
@@ -513,9 +515,13 @@ int srt_forward(const srt_fields* fields, int64_t nside, int64_t pix_begin, int6
     }
     if (timed || !dev_out) SRT_CUDA_TRY(cudaStreamSynchronize(s), "trace");
     if (stats) {
-      float ms = -1.f;
-      if (timed) cudaEventElapsedTime(&ms, e0, e1);
+      float ms = -1.f, rms = 0.f;
+      if (timed) {
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventElapsedTime(&rms, em, e1);
+      }
       stats->trace_ms = ms;
+      stats->retrace_ms = refine ? rms : 0.0;
       stats->rays = pix_count;
       stats->ray_steps = pix_count * (int64_t)n_steps;
       stats->kernels = kernels;
@@ -534,6 +540,7 @@ fail:
   if (refine_count) cudaFreeAsync(refine_count, s);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
+  if (em) cudaEventDestroy(em);
   if (prev != f->device) cudaSetDevice(prev);
   if (stats) stats->total_ms = wall.ms();
   return rc;

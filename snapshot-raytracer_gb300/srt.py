@@ -43,7 +43,7 @@ class SrtError(RuntimeError):
 class Stats(ctypes.Structure):
     _fields_ = [("trace_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("rays", ctypes.c_int64),
                 ("ray_steps", ctypes.c_int64), ("kernels", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64),
-                ("d2h_bytes", ctypes.c_int64), ("refined_rays", ctypes.c_int64)]
+                ("d2h_bytes", ctypes.c_int64), ("refined_rays", ctypes.c_int64), ("retrace_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

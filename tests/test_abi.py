@@ -25,7 +25,7 @@ def test_exports_every_declared_symbol(srt):
 
 
 def test_abi_version(srt):
-    assert srt.lib().srt_abi_version() == 3
+    assert srt.lib().srt_abi_version() == 4
 
 
 def test_forward_rejects_bad_arguments(srt):
@@ -86,7 +86,7 @@ int main(void) {
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     ver, rc, msg = r.stdout.split(" ", 2)
-    assert int(ver) == 3
+    assert int(ver) == 4
     if has_gpu():
         assert int(rc) == 0
     else:
