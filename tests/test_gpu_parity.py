@@ -192,6 +192,8 @@ def test_mixed_refines_face_crossing_rays(srt, orc):
         mr, st = f.forward(nside, steps, precision="mixed")
         mn, st0 = f.forward(nside, steps, precision="mixed", refine=False)
     assert st.refined_rays > 0 and st0.refined_rays == 0  # ~1e-3 of the rays at this size
+    # the re-trace's device time is reported as its share of trace_ms
+    assert 0.0 < st.retrace_ms < st.trace_ms and st0.retrace_ms == 0.0
     assert st.refined_rays < 0.01 * 12 * nside * nside
     same = np.all(mr.view(np.uint32) == m64.view(np.uint32), axis=0)
     changed = np.any(mr.view(np.uint32) != mn.view(np.uint32), axis=0)
