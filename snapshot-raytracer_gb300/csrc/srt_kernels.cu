@@ -309,26 +309,13 @@ __device__ __forceinline__ void rhs_dd_group(const dd* y, dd* dy, const FieldPtr
   rhs_finish<dd, dd>(y, n, a, b, B, r, dy, GroupDiv<dd>{field, group, gmask});
 }
 
-__device__ __forceinline__ void step_dd_group(const FieldPtrs& F, const Geom& G, dd* y, int field, int group,
-                                              unsigned mask) {
-  dd acc[19], k[19], ys[19];
-#pragma unroll 1
-  for (int st = 0; st < 4; ++st) {
-    const float c = (st == 3) ? 1.f : 0.5f;
-    for (int j = 0; j < 19; ++j) ys[j] = (st == 0) ? y[j] : y[j] + c * k[j];
-    rhs_dd_group(ys, k, F, G, field, group, mask);
-    for (int j = 0; j < 19; ++j) acc[j] = (st == 0) ? k[j] : ((st < 3) ? acc[j] + 2.f * k[j] : acc[j]);
-  }
-  const dd sixth = dd(1.0 / 6.0);
-  for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
-}
-
-// step_dd_group with the state and the RK4 accumulator in shared memory, one
-// copy per lane group (the four lanes of a group form the same values, so
-// each writes what the others write): the registers then hold only the stage
-// input, the stage's k and the right-hand side's working set.
-__device__ __forceinline__ void step_dd_group_sm(const FieldPtrs& F, const Geom& G, dd* y, dd* acc, int field,
-                                                 int group, unsigned mask) {
+// step_std<kFP64> in double-float on rhs_dd_group, with the state and the RK4
+// accumulator in shared memory, one copy per lane group (the four lanes of a
+// group form the same values, so each writes what the others write): the
+// registers then hold only the stage input, the stage's k and the right-hand
+// side's working set.
+__device__ __forceinline__ void step_dd_group(const FieldPtrs& F, const Geom& G, dd* y, dd* acc, int field,
+                                              int group, unsigned mask) {
   dd k[19];
 #pragma unroll 1
   for (int st = 0; st < 4; ++st) {
@@ -342,14 +329,15 @@ __device__ __forceinline__ void step_dd_group_sm(const FieldPtrs& F, const Geom&
   for (int j = 0; j < 19; ++j) y[j] += (acc[j] + k[j]) * sixth;
 }
 
-// step_dd_group with one lane doing the whole ray (rhs_dd: all four
-// interpolations and the right-hand side once).
 // One lane's double-float state in a shared-memory column of a warp's array
 // (component j at c[32 j]).
 struct DdCol {
   dd* c;
   __device__ dd& operator[](int j) const { return c[32 * j]; }
 };
+
+// step_dd_group with one lane doing the whole ray (rhs_dd: all four
+// interpolations and the right-hand side once), its state in a DdCol.
 
 __device__ __forceinline__ void step_dd1(const FieldPtrs& F, const Geom& G, const DdCol& y, const DdCol& acc) {
   dd k[19], ys[19];
@@ -438,7 +426,7 @@ __global__ void __launch_bounds__(32, (MODE == 1 || MODE == 2) ? 12 : 1)
       const unsigned mask = (live >= kRays) ? 0xffffffffu : ((1u << (4 * live)) - 1u);
 #pragma unroll 1
       for (int step = 0; step < A.n_steps; ++step)
-        step_dd_group_sm(A.F, A.G, y, reinterpret_cast<dd*>(s_acc[lane >> 2]), lane & 3, lane & ~3, mask);
+        step_dd_group(A.F, A.G, y, reinterpret_cast<dd*>(s_acc[lane >> 2]), lane & 3, lane & ~3, mask);
       {
         dd yl[19];
         for (int j = 0; j < 19; ++j) yl[j] = y[j];
