@@ -915,12 +915,15 @@ SRT_HD void rhs_mixed(const float* d, float s, const MixedRay& R, const FieldPtr
   for (int i = 0; i < 6; ++i) A.T[i] = 0.f;
   add_b_component<0, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
   add_b_component<1, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
-  add_b_component<2, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
+  // phi between the second and third B components: the same values in any
+  // order (the B sums keep theirs), and this one schedules best (1.0 % over
+  // phi last, 3 % over phi first, on the 1024^3 trace)
   Tri<float> p;
   if (PAIR)
     tricubic_pair(PairRows{F.pr[3], cell_base_pair(G, cc[0], cc[1], cc[2]), G.px, G.pxy2}, Cx, Cy, Cz, p);
   else
     tricubic_pair(SingleRows{F.phi, cell_base(G, cc[0], cc[1], cc[2]), G.px, G.pxy}, Cx, Cy, Cz, p);
+  add_b_component<2, PAIR>(F, G, cc, cs, ts, Cx, Cy, Cz, n, a, b, A);
 
   const float dA = s + d[12];
   const float dAp = d[13] - 1.f;
