@@ -1,10 +1,13 @@
-// Host build of the MIXED form's cell lookup (snapshot-raytracer_gb300/csrc/srt_scheme.cuh,
-// locate_mixed) for tests/test_locate_mixed.py.
+// Host build of the MIXED form's cell lookup and normalisation term
+// (snapshot-raytracer_gb300/csrc/srt_scheme.cuh: locate_mixed, rsqrt1p_m1) for
+// tests/test_locate_mixed.py.
 #include "srt_scheme.cuh"
 extern "C" {
 void locate(float th, float lo, int n, int* cc, float* tc, int* cs, float* ts, float* df) {
   srt::locate_mixed(th, lo, n, 1.0f / (float)n, *cc, *tc, *cs, *ts, *df);
 }
+// (1 + q)^(-1/2) - 1 as the MIXED form's normalisation takes it
+float rsqrt1p_m1(float q) { return srt::rsqrt1p_m1(q); }
 }
 
 // The MIXED trace of RING pixels [ring_begin, ring_begin + count) on the host,

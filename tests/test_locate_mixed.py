@@ -33,6 +33,8 @@ def loc(tmp_path_factory):
     if r.returncode != 0:
         pytest.skip("g++ failed: " + r.stderr[-300:])
     L = ctypes.CDLL(out)
+    L.rsqrt1p_m1.argtypes = [ctypes.c_float]
+    L.rsqrt1p_m1.restype = ctypes.c_float
     PI, PF = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
     L.locate.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int, PI, PF, PI, PF, PF]
 
@@ -43,6 +45,7 @@ def loc(tmp_path_factory):
                  ctypes.byref(df))
         return cc.value, tc.value, cs.value, ts.value, df.value
 
+    call.rsqrt1p_m1 = L.rsqrt1p_m1
     return call
 
 
@@ -135,3 +138,25 @@ def test_unresolvable_and_non_finite_positions_stay_in_range(loc):
             for lo in (0.0, 1e-3, -1e-3, nan):
                 cc, tc, cs, ts, df = loc(th, lo, n)
                 assert 0 <= cc < n and 0 <= cs < n, (th, lo, n, cc, cs)
+
+
+def test_normalisation_term_without_cancellation(loc):
+    """rsqrt1p_m1(q) = (1 + q)^(-1/2) - 1, the correction that keeps a
+    perturbed unit vector unit, in the closed form -q / (s (1 + s)),
+    s = (1 + q)^(1/2): no cancellation for the tiny q of the perturbation
+    form (|q| ~ 1e-5 and far below) nor for large q, so its relative error
+    stays at a few float ulps everywhere (host build, IEEE sqrt and division;
+    the GPU build's fast-math sqrt and division add ~2 ulps)."""
+    rng = np.random.default_rng(3)
+    qs = np.concatenate([np.float32(np.sign(rng.standard_normal(400)) * 10.0 ** rng.uniform(-30, -1, 400)),
+                         np.float32(rng.uniform(-0.9, 10.0, 200)), np.float32([0.0])])
+    worst = 0.0
+    for q in qs:
+        got = loc.rsqrt1p_m1(float(q))
+        sq = math.sqrt(1.0 + float(q))  # float q is exact in double
+        exact = -float(q) / (sq * (1.0 + sq))  # no cancellation: ~1e-16 relative
+        if q == 0.0:
+            assert got == 0.0
+            continue
+        worst = max(worst, abs(got - exact) / abs(exact))
+    assert worst < 4 * 2.0 ** -23, worst
