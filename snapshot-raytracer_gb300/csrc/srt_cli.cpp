@@ -291,12 +291,13 @@ int main(int argc, char* argv[]) {
   if (timing) {
     // read_*: the reader thread; layout_ms: copies and layout, overlapped with
     // the reads; after_read_ms: from the end of the reads to the fields being
-    // ready (what the upload adds to the reads)
+    // ready (what the upload adds to the reads); trace_kernel_ms: the trace
+    // and re-trace launches (device time), retrace_ms the re-trace's share
     printf("{\"read_phi_ms\": %.3f, \"read_b_ms\": %.3f, \"layout_ms\": %.3f, \"after_read_ms\": %.3f, "
-           "\"load_ms\": %.3f, \"trace_ms\": %.3f, \"trace_kernel_ms\": %.3f, \"write_ms\": %.3f, "
-           "\"total_ms\": %.3f, \"rays\": %lld, \"ray_steps\": %lld}\n",
+           "\"load_ms\": %.3f, \"trace_ms\": %.3f, \"trace_kernel_ms\": %.3f, \"retrace_ms\": %.3f, "
+           "\"write_ms\": %.3f, \"total_ms\": %.3f, \"rays\": %lld, \"ray_steps\": %lld}\n",
            ls.read_phi_ms, ls.read_b_ms, ls.layout_ms, ls.after_read_ms, t_up - t_start, t_trace - t_up, st.trace_ms,
-           t_end - t_trace, t_end - t_start, (long long)st.rays, (long long)st.ray_steps);
+           st.retrace_ms, t_end - t_trace, t_end - t_start, (long long)st.rays, (long long)st.ray_steps);
   }
   return 0;
 }
